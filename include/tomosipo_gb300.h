@@ -1,0 +1,107 @@
+/*
+ * tomosipo_gb300 -- C ABI of the GB300 (sm_103a) tomographic projector.
+ *
+ * This library replaces the link layer of tomosipo, ``tomosipo/astra.py``,
+ * which hands projection work to ASTRA's ``cuda3d`` projector. Every entry
+ * point takes plain pointers and sizes; no C++ or PyTorch types cross the ABI.
+ * Entry points return TSGB_OK (0) or a negative error code and never throw;
+ * ``tsgb_last_error`` gives a message for the calling thread's last failure.
+ *
+ * Layouts (tomosipo's, ``tomosipo/links/base.py:21-31``):
+ *   volume   : float32 [Nz][Ny][Nx], C-contiguous, x fastest
+ *   sinogram : float32 [rows][num_angles][cols], C-contiguous, u fastest
+ * All device pointers must be on the device the projector was created on.
+ * Work is queued on ``stream`` (a cudaStream_t; NULL = legacy default
+ * stream) and is asynchronous with respect to the host.
+ */
+#ifndef TOMOSIPO_GB300_H
+#define TOMOSIPO_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define TSGB_OK 0
+#define TSGB_ERR_INVALID (-1)   /* bad argument, shape or geometry */
+#define TSGB_ERR_CUDA (-2)      /* a CUDA runtime call failed */
+#define TSGB_ERR_WORKSPACE (-3) /* workspace missing or too small */
+#define TSGB_ERR_DEVICE (-4)    /* current device differs from the projector's */
+
+#define TSGB_PARALLEL 0 /* rows of ``vectors`` start with a ray direction */
+#define TSGB_CONE 1     /* rows of ``vectors`` start with a source position */
+
+#define TSGB_BP_MATCHED 0  /* exact transpose of the forward projector */
+#define TSGB_BP_BILINEAR 1 /* voxel-driven, bilinear detector interpolation */
+
+/* Axis-aligned volume: the form ``ts.operator`` reduces every volume to
+ * (``tomosipo/Operator.py:11-60``) before it builds a projector. */
+typedef struct {
+  int64_t shape[3]; /* voxels (z, y, x) */
+  double pos[3];    /* centre (z, y, x) */
+  double size[3];   /* physical size (z, y, x) */
+} tsgb_volume_desc;
+
+/* Projection geometry in vector form (``pg.to_vec()``). Row ``t`` of
+ * ``vectors`` (num_angles x 12 doubles) is
+ *   [ src_pos or ray_dir (z,y,x), det_pos (z,y,x), det_v (z,y,x), det_u (z,y,x) ]
+ * with det_pos the detector centre and det_v / det_u one pixel up / across
+ * (``tomosipo/geometry/cone_vec.py``, ``parallel_vec.py``). */
+typedef struct {
+  int32_t kind;         /* TSGB_PARALLEL or TSGB_CONE */
+  int32_t reserved;
+  int64_t det_shape[2]; /* rows, cols */
+  int64_t num_angles;
+  const double* vectors;
+} tsgb_projection_desc;
+
+typedef struct tsgb_projector tsgb_projector;
+
+/* Build a projector for one volume/projection geometry pair on the current
+ * CUDA device. Replaces ``create_astra_projector`` (tomosipo/astra.py:80-98).
+ * Supersampling factors must be >= 1 (1 = none): detector supersampling d
+ * averages d*d rays per pixel in the forward projection (and its transpose);
+ * voxel supersampling d averages d*d*d points per voxel in the bilinear
+ * backprojection. Allocates the per-angle tables on the device. */
+int tsgb_projector_create(const tsgb_volume_desc* vol,
+                          const tsgb_projection_desc* proj,
+                          int32_t voxel_supersampling,
+                          int32_t detector_supersampling,
+                          tsgb_projector** out);
+
+/* Free a projector (ASTRA: astra.projector3d.delete; the reference leaves it
+ * to garbage collection). Synchronises the projector's device. */
+int tsgb_projector_destroy(tsgb_projector* p);
+
+/* Bytes of device workspace ``tsgb_direct_fp`` / ``tsgb_direct_bp`` need. */
+int64_t tsgb_fp_workspace_bytes(const tsgb_projector* p);
+int64_t tsgb_bp_workspace_bytes(const tsgb_projector* p, int32_t bp_kind);
+
+/* Forward projection sino = A(vol), or sino += A(vol) when ``additive``.
+ * Replaces ``direct_fp`` -> ``astra.experimental.direct_FPBP3D(projector,
+ * vol, proj, MODE_SET|MODE_ADD, "FP")`` (tomosipo/astra.py:104-184). */
+int tsgb_direct_fp(tsgb_projector* p, const float* vol, float* sino,
+                   int32_t additive, void* workspace, int64_t workspace_bytes,
+                   void* stream);
+
+/* Backprojection vol = A^T(sino) (bp_kind TSGB_BP_MATCHED) or its
+ * voxel-driven bilinear approximation (TSGB_BP_BILINEAR); vol += ... when
+ * ``additive``. Replaces ``direct_bp`` -> ``direct_FPBP3D(..., "BP")``
+ * (tomosipo/astra.py:187-217). */
+int tsgb_direct_bp(tsgb_projector* p, float* vol, const float* sino,
+                   int32_t additive, int32_t bp_kind, void* workspace,
+                   int64_t workspace_bytes, void* stream);
+
+/* Shapes the projector expects: vol (z, y, x) and sino (rows, angles, cols). */
+int tsgb_projector_shapes(const tsgb_projector* p, int64_t vol_shape[3],
+                          int64_t sino_shape[3]);
+
+/* Message for the calling thread's most recent error ("" if none). */
+const char* tsgb_last_error(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* TOMOSIPO_GB300_H */

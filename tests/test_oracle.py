@@ -1,0 +1,131 @@
+"""The FP64 oracle against known answers, the reference's one numeric output,
+and the committed golden fixtures (CPU only)."""
+import json
+import os
+
+import numpy as np
+import pytest
+
+import tomosipo_gb300 as ts
+from oracle import oracle as orc
+from tests.helpers import adjoint_error, ellipsoid_phantom, rel_l2
+
+GOLDEN = os.path.join(os.path.dirname(__file__), "golden")
+
+
+def test_parallel_chord_length_unit_cube():
+    # A ray along an axis through a unit cube of ones integrates to 1.0.
+    vg = ts.volume(shape=16, size=1)
+    pg = ts.parallel(angles=[0.0, np.pi / 2], shape=(16, 24), size=(1, 1.5))
+    y = orc.fp(vg, pg, np.ones(vg.shape))
+    inside = y[:, :, 4:20]
+    assert np.allclose(inside, 1.0)
+    assert np.allclose(y[:, :, :3], 0.0) and np.allclose(y[:, :, 21:], 0.0)
+
+
+def test_parallel_diagonal_chord():
+    # At 45 degrees a ray at perpendicular offset d from the centre has chord sqrt2 - 2d.
+    n = 64
+    vg = ts.volume(shape=(1, n, n), size=(1.0 / n, 1, 1))
+    pg = ts.parallel(angles=[np.pi / 4], shape=(1, 2 * n), size=(1.0 / n, 2.0))
+    y = orc.fp(vg, pg, np.ones(vg.shape))[0, 0]
+    su = 2.0 / (2 * n)
+    for iu in range(n - 8, n + 8):
+        d = abs((iu + 0.5 - n) * su)
+        assert y[iu] == pytest.approx(np.sqrt(2) - 2 * d, abs=2e-3)
+
+
+def test_cone_central_ray_chord():
+    # The cone ray through the volume centre along an axis has chord = volume size.
+    vg = ts.volume(shape=16, size=1)
+    pg = ts.cone(angles=[0.0], shape=(15, 15), size=1.5, src_orig_dist=3, src_det_dist=4)
+    y = orc.fp(vg, pg, np.ones(vg.shape))
+    assert y[7, 0, 7] == pytest.approx(1.0, abs=1e-12)
+
+
+@pytest.mark.parametrize("cone", [False, True])
+def test_oracle_adjoint(cone):
+    vg = ts.volume(shape=(12, 14, 16), size=(1, 1.2, 1.1))
+    pg = (
+        ts.cone(angles=9, shape=(13, 17), size=2, src_orig_dist=3, src_det_dist=4)
+        if cone
+        else ts.parallel(angles=9, shape=(13, 17), size=2)
+    )
+    rng = np.random.default_rng(1)
+    x = rng.random(vg.shape)
+    y = rng.random((13, 9, 17))
+    for ss in (1, 2):
+        Ax = orc.fp(vg, pg, x, det_ss=ss)
+        ATy = orc.bp_matched(vg, pg, y, det_ss=ss)
+        assert adjoint_error(Ax, y, x, ATy) < 1e-13
+
+
+@pytest.mark.parametrize("cone,band", [(False, 0.03), (True, 0.2)])
+def test_bilinear_approximates_matched(cone, band):
+    """The bilinear backprojector approximates the transpose: equal totals (both
+    spread each ray's value over voxel volume / pixel area), and close values.
+    In cone beams the matched transpose aliases where rays are sparser than
+    voxels (beyond the detector plane here), hence the wider band."""
+    vg = ts.volume(shape=32, size=1)
+    pg = (
+        ts.cone(angles=32, shape=(32, 48), size=np.sqrt(2), cone_angle=0.5)
+        if cone
+        else ts.parallel(angles=32, shape=(32, 48), size=(1, 1.5))
+    )
+    x = ellipsoid_phantom(vg.shape, n=6, seed=2).astype(np.float64)
+    y = orc.fp(vg, pg, x)
+    bb, bm = orc.bp_bilinear(vg, pg, y), orc.bp_matched(vg, pg, y)
+    assert bb.sum() == pytest.approx(bm.sum(), rel=1e-3)
+    assert rel_l2(bb, bm) < band
+
+
+@pytest.mark.parametrize("cone", [False, True])
+def test_detector_supersampling_is_binned_fine_detector(cone):
+    """d x d rays per pixel == the plain projection onto a d-times finer detector,
+    averaged over d x d blocks (exact identity of the discretisation)."""
+    vg = ts.volume(shape=(12, 14, 16), size=1)
+    pg = (
+        ts.cone(angles=5, shape=(9, 11), size=(1.3, 1.7), src_orig_dist=3, src_det_dist=4)
+        if cone
+        else ts.parallel(angles=5, shape=(9, 11), size=(1.3, 1.7))
+    )
+    x = np.random.default_rng(4).random(vg.shape)
+    for d in (2, 3):
+        fine = orc.fp(vg, pg.to_vec().reshape((9 * d, 11 * d)), x)
+        binned = fine.reshape(9, d, 5, 11, d).mean(axis=(1, 4))
+        assert rel_l2(orc.fp(vg, pg, x, det_ss=d), binned) < 1e-12
+
+
+def test_reference_notebook_hollow_box_pin():
+    """notebooks/cupy.ipynb cell 4 (reference, ASTRA on GPU): hollow box on a 128^3
+    unit cube, ts.parallel(angles=180, shape=128): sinogram mean 0.109146185,
+    max 0.8471311. The old-API detector size is not printed; size sqrt(2) is the
+    one consistent with the mean. The mean depends only on the world-unit scaling
+    (line integrals / pixel area), the max also on the interpolation (ASTRA uses
+    fixed-point texture weights), so it gets the 5e-3 ASTRA band."""
+    with open(os.path.join(GOLDEN, "reference_pins.json")) as f:
+        pin = json.load(f)["cupy_notebook_hollow_box"]
+    vg = ts.volume(shape=128, size=1)
+    x = np.zeros(vg.shape)
+    ts.phantom.hollow_box(x)
+    assert x.mean() == pytest.approx(pin["volume_mean"], rel=1e-6)
+    pg = ts.parallel(angles=180, shape=128, size=np.sqrt(2))
+    y = orc.fp(vg, pg, x)
+    assert y.mean() == pytest.approx(pin["sino_mean"], rel=1e-4)
+    assert y.max() == pytest.approx(pin["sino_max"], rel=5e-3)
+
+
+def _golden_cases():
+    with open(os.path.join(GOLDEN, "cases.json")) as f:
+        return json.load(f)
+
+
+@pytest.mark.parametrize("name", sorted(_golden_cases()))
+def test_oracle_matches_golden_fixture(name):
+    from tests.golden.make_golden import build_case
+
+    vg, pg, x, y = build_case(name)
+    data = np.load(os.path.join(GOLDEN, f"{name}.npz"))
+    assert rel_l2(orc.fp(vg, pg, x), data["fp"]) < 1e-12
+    assert rel_l2(orc.bp_matched(vg, pg, y), data["bp_matched"]) < 1e-12
+    assert rel_l2(orc.bp_bilinear(vg, pg, y), data["bp_bilinear"]) < 1e-12

@@ -1,0 +1,153 @@
+"""Parity of the sm_103a projector with the FP64 oracle, through the public API.
+
+Every case runs forward projection, matched backprojection and bilinear
+backprojection on the GPU (ts.operator -> C ABI -> kernels) and compares
+them with the oracle on the same seeded inputs. Gates: relative L2 error
+<= 1e-5 (TOL_ORACLE) and adjointness <= 1e-6 (TOL_ADJOINT).
+"""
+import numpy as np
+import pytest
+
+import tomosipo_gb300 as ts
+from oracle import oracle as orc
+from tests.helpers import (
+    TOL_ADJOINT,
+    TOL_ORACLE,
+    adjoint_error,
+    ellipsoid_phantom,
+    helical_cone_vec,
+    noise_cube_phantom,
+    rel_l2,
+)
+
+torch = pytest.importorskip("torch")
+pytestmark = pytest.mark.gpu
+
+
+def _cases():
+    rng = np.random.default_rng(7)
+    R = ts.rotate(pos=0, axis=rng.normal(size=3), angles=0.7)
+    R2 = ts.rotate(pos=0, axis=(1.0, 0.3, -0.2), angles=0.4)
+    vg32 = ts.volume(shape=32, size=1)
+    return {
+        "parallel": (vg32, ts.parallel(angles=24, shape=(32, 48), size=(1, 1.5))),
+        "cone": (vg32, ts.cone(angles=24, shape=(32, 48), size=np.sqrt(2), cone_angle=0.5)),
+        "parallel_aniso": (
+            ts.volume(shape=(20, 28, 36), size=(0.7, 1.1, 1.3), pos=(0.05, -0.1, 0.2)),
+            ts.parallel(angles=np.linspace(0.1, 3.0, 13), shape=(17, 29), size=(1.2, 2.1)),
+        ),
+        "cone_aniso": (
+            ts.volume(shape=(20, 28, 36), size=(0.7, 1.1, 1.3), pos=(0.05, -0.1, 0.2)),
+            ts.cone(angles=11, shape=(19, 31), size=(1.5, 2.5), src_orig_dist=3.0, src_det_dist=4.5),
+        ),
+        "cone_vec_helical": (
+            vg32,
+            helical_cone_vec(40, (24, 40), (1.0, 1.6), 2.5, 1.0, pitch=0.3, turns=1.5,
+                             jitter=0.5, voxel=1 / 32),
+        ),
+        "parallel_vec_rotated": (vg32, R * ts.parallel(angles=16, shape=(40, 48), size=(1.4, 1.6)).to_vec()),
+        "cone_vec_rotated": (
+            vg32,
+            R2 * ts.cone(angles=12, shape=(36, 44), size=1.6, src_orig_dist=2.5, src_det_dist=3.5).to_vec(),
+        ),
+        "parallel_45deg": (vg32, ts.parallel(angles=[np.pi / 4, 3 * np.pi / 4, 0.0], shape=(32, 48), size=(1, 1.5))),
+        "one_angle_one_row": (vg32, ts.cone(angles=[0.3], shape=(1, 48), size=(0.1, 1.5), src_orig_dist=3, src_det_dist=3)),
+        "small_detector": (vg32, ts.parallel(angles=9, shape=(8, 8), size=(0.3, 0.3))),
+    }
+
+
+CASES = _cases()
+
+
+@pytest.fixture(scope="module")
+def device(native_lib):
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    return torch.device("cuda", 0)
+
+
+@pytest.mark.parametrize("name", sorted(CASES))
+def test_fp_bp_parity(name, device):
+    vg, pg = CASES[name]
+    A = ts.operator(vg, pg)
+    x = noise_cube_phantom(vg.shape, seed=11)
+    y_gpu = A(torch.from_numpy(x).to(device)).cpu().numpy()
+    y_ref = orc.fp(vg, pg, x)
+    assert y_gpu.shape == y_ref.shape == A.range_shape
+    assert rel_l2(y_gpu, y_ref) <= TOL_ORACLE, rel_l2(y_gpu, y_ref)
+
+    rng = np.random.default_rng(12)
+    yy = rng.random(A.range_shape).astype(np.float32)
+    x_gpu = A.T(torch.from_numpy(yy).to(device)).cpu().numpy()
+    x_ref = orc.bp_matched(vg, pg, yy)
+    assert rel_l2(x_gpu, x_ref) <= TOL_ORACLE, rel_l2(x_gpu, x_ref)
+    assert adjoint_error(y_gpu, yy, x, x_gpu) <= TOL_ADJOINT
+
+    B = ts.operator(vg, pg, backprojector="bilinear")
+    xb_gpu = B.T(torch.from_numpy(yy).to(device)).cpu().numpy()
+    xb_ref = orc.bp_bilinear(vg, pg, yy)
+    assert rel_l2(xb_gpu, xb_ref) <= TOL_ORACLE, rel_l2(xb_gpu, xb_ref)
+
+
+def test_minimum_slice_parallel64(device):
+    """Plain parallel3d: 64^3 unit cube, noise + unit cube, 96 angles, detector 64x96."""
+    vg = ts.volume(shape=64, size=1)
+    pg = ts.parallel(angles=96, shape=(64, 96), size=(1, 1.5))
+    A = ts.operator(vg, pg)
+    x = noise_cube_phantom(vg.shape, seed=0)
+    y = A(torch.from_numpy(x).to(device))
+    y_ref = orc.fp(vg, pg, x)
+    assert rel_l2(y.cpu().numpy(), y_ref) <= TOL_ORACLE
+    bp = A.T(y)
+    bp_ref = orc.bp_matched(vg, pg, y.cpu().numpy())
+    assert rel_l2(bp.cpu().numpy(), bp_ref) <= TOL_ORACLE
+    rng = np.random.default_rng(3)
+    yy = torch.from_numpy(rng.random(A.range_shape).astype(np.float32)).to(device)
+    assert adjoint_error(y.cpu(), yy.cpu(), x, A.T(yy).cpu()) <= TOL_ADJOINT
+
+
+def test_cone_256_subset_parity(device):
+    """Cone 256^3 (size sqrt2, cone angle 0.5, detector 256x384) on 6 of 360 angles."""
+    vg = ts.volume(shape=256, size=1)
+    full = ts.cone(angles=360, shape=(256, 384), size=np.sqrt(2), cone_angle=0.5)
+    pg = full[::60]
+    A = ts.operator(vg, pg)
+    x = ellipsoid_phantom(vg.shape, seed=1)
+    y = A(torch.from_numpy(x).to(device)).cpu().numpy()
+    y_ref = orc.fp(vg, pg, x)
+    assert rel_l2(y, y_ref) <= TOL_ORACLE, rel_l2(y, y_ref)
+    bp = A.T(torch.from_numpy(y).to(device)).cpu().numpy()
+    bp_ref = orc.bp_matched(vg, pg, y)
+    assert rel_l2(bp, bp_ref) <= TOL_ORACLE, rel_l2(bp, bp_ref)
+
+
+def test_additive_is_twice(device):
+    """tests/test_Operator.py:35-49: applying an additive operator twice = 2 A(x)."""
+    vg = ts.volume(shape=40)
+    pg = ts.cone(size=np.sqrt(2) * 40, cone_angle=1 / 2, angles=30, shape=40)
+    A = ts.operator(vg, pg, additive=False)
+    B = ts.operator(vg, pg, additive=True)
+    x = torch.zeros(A.domain_shape, device=device)
+    ts.phantom.hollow_box(x)
+    y = torch.zeros(A.range_shape, device=device)
+    B(x, out=y)
+    B(x, out=y)
+    assert torch.allclose(2 * A(x), y, rtol=1e-6, atol=1e-6)
+    v = torch.zeros(A.domain_shape, device=device)
+    B.T(y, out=v)
+    B.T(y, out=v)
+    assert torch.allclose(2 * A.T(y), v, rtol=1e-6, atol=1e-5)
+
+
+def test_numpy_and_torch_inputs_agree(device):
+    """tests/test_Operator.py:15-32: the array type does not change the result."""
+    vg = ts.volume(shape=48)
+    pg = ts.cone(size=np.sqrt(2) * 48, cone_angle=1 / 2, angles=40, shape=48)
+    A = ts.operator(vg, pg)
+    x = np.zeros(A.domain_shape, dtype=np.float32)
+    ts.phantom.hollow_box(x)
+    y_np = A(x)
+    y_t = A(torch.from_numpy(x).to(device)).cpu().numpy()
+    assert isinstance(y_np, np.ndarray)
+    assert np.abs(y_np - y_t).sum() == pytest.approx(0.0)
+    assert np.abs(A.T(y_np) - A.T(torch.from_numpy(y_t).to(device)).cpu().numpy()).sum() == pytest.approx(0.0, abs=1e-3)

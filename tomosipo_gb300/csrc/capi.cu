@@ -1,0 +1,178 @@
+// extern "C" entry points of libtomosipo_gb300 (declared in include/tomosipo_gb300.h).
+#include <cuda_runtime.h>
+
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "tsgb_internal.h"
+
+namespace {
+
+thread_local std::string g_last_error;
+
+int fail(int code, const std::string& msg) {
+  g_last_error = msg;
+  return code;
+}
+
+int cuda_fail(cudaError_t e, const char* what) {
+  return fail(TSGB_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+void free_device(tsgb_projector* p) {
+  if (p->d_params) cudaFree(p->d_params);
+  if (p->d_columns) cudaFree(p->d_columns);
+  if (p->d_sep_angles) cudaFree(p->d_sep_angles);
+  if (p->d_gen_angles) cudaFree(p->d_gen_angles);
+  p->d_params = nullptr;
+  p->d_columns = nullptr;
+  p->d_sep_angles = nullptr;
+  p->d_gen_angles = nullptr;
+}
+
+template <typename T>
+cudaError_t upload(T** dst, const std::vector<T>& src) {
+  const size_t bytes = (src.empty() ? 1 : src.size()) * sizeof(T);
+  cudaError_t e = cudaMalloc(reinterpret_cast<void**>(dst), bytes);
+  if (e != cudaSuccess) return e;
+  if (!src.empty()) e = cudaMemcpy(*dst, src.data(), src.size() * sizeof(T), cudaMemcpyHostToDevice);
+  return e;
+}
+
+int check_device(const tsgb_projector* p) {
+  int dev = -1;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaGetDevice");
+  if (dev != p->device)
+    return fail(TSGB_ERR_DEVICE, "current CUDA device " + std::to_string(dev) +
+                                     " differs from the projector's device " +
+                                     std::to_string(p->device));
+  return TSGB_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int tsgb_projector_create(const tsgb_volume_desc* vol, const tsgb_projection_desc* proj,
+                          int32_t voxel_supersampling, int32_t detector_supersampling,
+                          tsgb_projector** out) {
+  g_last_error.clear();
+  if (!out) return fail(TSGB_ERR_INVALID, "out is NULL");
+  *out = nullptr;
+  tsgb_projector* p = new (std::nothrow) tsgb_projector();
+  if (!p) return fail(TSGB_ERR_INVALID, "host allocation failed");
+  std::vector<tsgb::ColumnEntry> columns;
+  std::vector<int> sep, gen;
+  std::string err = tsgb::build_plan(vol, proj, voxel_supersampling, detector_supersampling, p,
+                                     &columns, &sep, &gen);
+  if (!err.empty()) {
+    delete p;
+    return fail(TSGB_ERR_INVALID, err);
+  }
+  for (const auto& L : p->layouts)
+    if (L.floats() >= (int64_t(1) << 31)) {
+      delete p;
+      return fail(TSGB_ERR_INVALID, "volume too large for 32-bit indexing of one padded copy");
+    }
+  if (p->g.nz > 65535 || p->g.rows > 4 * 65535) {
+    delete p;
+    return fail(TSGB_ERR_INVALID, "volume z extent must be <= 65535 and detector rows <= 262140");
+  }
+  cudaError_t e = cudaGetDevice(&p->device);
+  if (e == cudaSuccess) e = upload(&p->d_params, p->host_params);
+  if (e == cudaSuccess) e = upload(&p->d_columns, columns);
+  if (e == cudaSuccess) e = upload(&p->d_sep_angles, sep);
+  if (e == cudaSuccess) e = upload(&p->d_gen_angles, gen);
+  if (e != cudaSuccess) {
+    free_device(p);
+    delete p;
+    return cuda_fail(e, "projector upload");
+  }
+  *out = p;
+  return TSGB_OK;
+}
+
+int tsgb_projector_destroy(tsgb_projector* p) {
+  g_last_error.clear();
+  if (!p) return TSGB_OK;
+  int prev = -1;
+  cudaGetDevice(&prev);
+  if (prev != p->device) cudaSetDevice(p->device);
+  free_device(p);
+  if (prev >= 0 && prev != p->device) cudaSetDevice(prev);
+  delete p;
+  return TSGB_OK;
+}
+
+int64_t tsgb_fp_workspace_bytes(const tsgb_projector* p) {
+  if (!p) return fail(TSGB_ERR_INVALID, "projector is NULL");
+  return p->fp_workspace_floats * int64_t(sizeof(float));
+}
+
+int64_t tsgb_bp_workspace_bytes(const tsgb_projector* p, int32_t bp_kind) {
+  if (!p) return fail(TSGB_ERR_INVALID, "projector is NULL");
+  if (bp_kind == TSGB_BP_BILINEAR) return 0;
+  if (bp_kind != TSGB_BP_MATCHED) return fail(TSGB_ERR_INVALID, "unknown bp_kind");
+  return int64_t(p->g.rows) * p->g.nangles * p->g.cols * int64_t(sizeof(float));
+}
+
+int tsgb_projector_shapes(const tsgb_projector* p, int64_t vol_shape[3], int64_t sino_shape[3]) {
+  if (!p) return fail(TSGB_ERR_INVALID, "projector is NULL");
+  if (vol_shape) {
+    vol_shape[0] = p->g.nz;
+    vol_shape[1] = p->g.ny;
+    vol_shape[2] = p->g.nx;
+  }
+  if (sino_shape) {
+    sino_shape[0] = p->g.rows;
+    sino_shape[1] = p->g.nangles;
+    sino_shape[2] = p->g.cols;
+  }
+  return TSGB_OK;
+}
+
+int tsgb_direct_fp(tsgb_projector* p, const float* vol, float* sino, int32_t additive,
+                   void* workspace, int64_t workspace_bytes, void* stream) {
+  g_last_error.clear();
+  if (!p || !vol || !sino) return fail(TSGB_ERR_INVALID, "NULL projector or data pointer");
+  const int64_t need = tsgb_fp_workspace_bytes(p);
+  if (need > 0 && (!workspace || workspace_bytes < need))
+    return fail(TSGB_ERR_WORKSPACE, "forward projection needs " + std::to_string(need) +
+                                        " bytes of workspace");
+  int rc = check_device(p);
+  if (rc != TSGB_OK) return rc;
+  cudaError_t e = cudaError_t(
+      tsgb::launch_fp(p, vol, sino, additive != 0, static_cast<float*>(workspace), stream));
+  if (e != cudaSuccess) return cuda_fail(e, "forward projection launch");
+  return TSGB_OK;
+}
+
+int tsgb_direct_bp(tsgb_projector* p, float* vol, const float* sino, int32_t additive,
+                   int32_t bp_kind, void* workspace, int64_t workspace_bytes, void* stream) {
+  g_last_error.clear();
+  if (!p || !vol || !sino) return fail(TSGB_ERR_INVALID, "NULL projector or data pointer");
+  if (bp_kind != TSGB_BP_MATCHED && bp_kind != TSGB_BP_BILINEAR)
+    return fail(TSGB_ERR_INVALID, "unknown bp_kind");
+  const int64_t need = tsgb_bp_workspace_bytes(p, bp_kind);
+  if (need > 0 && (!workspace || workspace_bytes < need))
+    return fail(TSGB_ERR_WORKSPACE,
+                "backprojection needs " + std::to_string(need) + " bytes of workspace");
+  int rc = check_device(p);
+  if (rc != TSGB_OK) return rc;
+  cudaError_t e;
+  if (bp_kind == TSGB_BP_MATCHED)
+    e = cudaError_t(tsgb::launch_bp_matched(p, vol, sino, additive != 0,
+                                            static_cast<float*>(workspace), stream));
+  else
+    e = cudaError_t(tsgb::launch_bp_bilinear(p, vol, sino, additive != 0, stream));
+  if (e != cudaSuccess) return cuda_fail(e, "backprojection launch");
+  return TSGB_OK;
+}
+
+const char* tsgb_last_error(void) { return g_last_error.c_str(); }
+
+}  // extern "C"

@@ -1,0 +1,88 @@
+// Device helpers shared by the projector kernels.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "tsgb_internal.h"
+
+namespace tsgb {
+
+// Per-layout addressing of a padded forward-projection volume copy.
+// Element (k along d, i along a, j along b), all unpadded indices, lives at
+//   base + (j + kPad) * stride_b + k * stride_d + (i + kPad)
+// with stride_d = n_a + 2 kPad and stride_b = n_d * stride_d (a fastest).
+struct LayoutDev {
+  long long offset;
+  int n_d, n_a, n_b;
+  int o_d, o_a, o_b;
+  int stride_d, stride_b;
+};
+
+struct LayoutTable {
+  LayoutDev l[kMaxLayouts];
+  int count;
+};
+
+__host__ inline LayoutTable make_layout_table(const tsgb_projector* p) {
+  LayoutTable t{};
+  const int anchors[3] = {p->g.oz, p->g.oy, p->g.ox};
+  t.count = int(p->layouts.size());
+  for (int i = 0; i < t.count; ++i) {
+    const Layout& L = p->layouts[i];
+    LayoutDev& D = t.l[i];
+    D.offset = L.offset_floats;
+    D.n_d = int(L.n_d);
+    D.n_a = int(L.n_a);
+    D.n_b = int(L.n_b);
+    D.o_d = anchors[L.d];
+    D.o_a = anchors[L.a];
+    D.o_b = anchors[L.b];
+    D.stride_d = int(L.n_a + 2 * kPad);
+    D.stride_b = int(L.n_d * (L.n_a + 2 * kPad));
+  }
+  return t;
+}
+
+// Ray through anchored pixel (ut, vt) for one angle: in-plane position on
+// plane kt of the dominant axis is (Xa + kt ma, Xb + kt mb).
+struct Ray {
+  float Xa, ma, Xb, mb;
+};
+
+__device__ __forceinline__ Ray ray_general(const AngleParams& ap, float ut, float vt) {
+  const float den = fmaf(ap.e[2], vt, fmaf(ap.e[1], ut, ap.e[0]));
+  const float inv = 1.0f / den;
+  Ray r;
+  r.Xa = fmaf(ap.ca[2], vt, fmaf(ap.ca[1], ut, ap.ca[0])) * inv;
+  r.ma = fmaf(ap.ma[2], vt, fmaf(ap.ma[1], ut, ap.ma[0])) * inv;
+  r.Xb = fmaf(ap.cb[2], vt, fmaf(ap.cb[1], ut, ap.cb[0])) * inv;
+  r.mb = fmaf(ap.mb[2], vt, fmaf(ap.mb[1], ut, ap.mb[0])) * inv;
+  return r;
+}
+
+__device__ __forceinline__ Ray ray_column(const ColumnEntry& c, float vt) {
+  Ray r;
+  r.Xa = c.Xa;
+  r.ma = c.ma;
+  r.Xb = fmaf(vt, c.R, c.P);
+  r.mb = fmaf(vt, c.S, c.Q);
+  return r;
+}
+
+// World length of the ray between consecutive planes of the dominant axis.
+__device__ __forceinline__ float ray_step(const AngleParams& ap, const Ray& r) {
+  const float vd = ap.vs_d, va = ap.vs_a * r.ma, vb = ap.vs_b * r.mb;
+  return sqrtf(fmaf(vd, vd, fmaf(va, va, vb * vb)));
+}
+
+__device__ __forceinline__ float tent(float t) { return fmaxf(0.0f, 1.0f - fabsf(t)); }
+
+// Clamp a detector coordinate to +-1e8 before an int conversion (NaN -> -1e8,
+// +-inf -> +-1e8), so range bounds never overflow 32-bit integers.
+__device__ __forceinline__ float clamp_coord(float c) { return fminf(fmaxf(c, -1.0e8f), 1.0e8f); }
+
+__device__ __forceinline__ bool finite_ray(const Ray& r) {
+  return isfinite(r.Xa) && isfinite(r.ma) && isfinite(r.Xb) && isfinite(r.mb);
+}
+
+}  // namespace tsgb

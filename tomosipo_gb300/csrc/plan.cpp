@@ -1,0 +1,294 @@
+// Host-side (fp64) construction of the per-angle projector tables.
+//
+// Input is what tomosipo hands ASTRA in ``create_astra_projector``
+// (tomosipo/astra.py:80-98): an axis-aligned volume and the vector form of
+// the projection geometry. Everything here runs once per projector, in
+// double precision, and is rounded to fp32 only at the end so the kernels
+// start from correctly rounded coefficients.
+#include <cmath>
+#include <cstdio>
+#include <string>
+#include <vector>
+
+#include "tsgb_internal.h"
+
+namespace tsgb {
+namespace {
+
+struct V3 {
+  double c[3];
+  double& operator[](int i) { return c[i]; }
+  double operator[](int i) const { return c[i]; }
+};
+
+V3 sub(const V3& a, const V3& b) { return {{a[0] - b[0], a[1] - b[1], a[2] - b[2]}}; }
+double dot(const V3& a, const V3& b) { return a[0] * b[0] + a[1] * b[1] + a[2] * b[2]; }
+// Cross product on the stored components; only used inside ratios of triple
+// products, which do not depend on the handedness of the component order.
+V3 cross(const V3& a, const V3& b) {
+  return {{a[1] * b[2] - a[2] * b[1], a[2] * b[0] - a[0] * b[2], a[0] * b[1] - a[1] * b[0]}};
+}
+double norm(const V3& a) { return std::sqrt(dot(a, a)); }
+V3 scale(const V3& a, double s) { return {{a[0] * s, a[1] * s, a[2] * s}}; }
+V3 axpy(const V3& a, double s, const V3& b) {  // a + s * b
+  return {{a[0] + s * b[0], a[1] + s * b[1], a[2] + s * b[2]}};
+}
+
+int argmax_abs(const V3& v, int skip) {
+  int best = -1;
+  for (int i = 0; i < 3; ++i) {
+    if (i == skip) continue;
+    if (best < 0 || std::fabs(v[i]) > std::fabs(v[best])) best = i;
+  }
+  return best;
+}
+
+bool finite3(const V3& v) {
+  return std::isfinite(v[0]) && std::isfinite(v[1]) && std::isfinite(v[2]);
+}
+
+}  // namespace
+
+std::string build_plan(const tsgb_volume_desc* vol, const tsgb_projection_desc* proj,
+                       int voxel_ss, int det_ss, tsgb_projector* p,
+                       std::vector<ColumnEntry>* columns, std::vector<int>* sep_angles,
+                       std::vector<int>* gen_angles) {
+  if (!vol || !proj || !proj->vectors) return "null geometry descriptor";
+  if (proj->kind != TSGB_PARALLEL && proj->kind != TSGB_CONE)
+    return "projection kind must be TSGB_PARALLEL or TSGB_CONE";
+  if (voxel_ss < 1 || det_ss < 1 || voxel_ss > 16 || det_ss > 16)
+    return "supersampling factors must lie in [1, 16]";
+  for (int i = 0; i < 3; ++i) {
+    if (vol->shape[i] < 1 || vol->shape[i] > (1 << 20)) return "volume shape out of range";
+    if (!(vol->size[i] > 0) || !std::isfinite(vol->size[i]) || !std::isfinite(vol->pos[i]))
+      return "volume size must be positive and finite";
+  }
+  if (proj->det_shape[0] < 1 || proj->det_shape[1] < 1 || proj->det_shape[0] > (1 << 20) ||
+      proj->det_shape[1] > (1 << 20))
+    return "detector shape out of range";
+  if (proj->num_angles < 1 || proj->num_angles > (1 << 24)) return "number of angles out of range";
+  const int64_t nvox = vol->shape[0] * vol->shape[1] * vol->shape[2];
+  const int64_t nsino = proj->det_shape[0] * proj->det_shape[1] * proj->num_angles;
+  if (nvox > (int64_t(1) << 40) || nsino > (int64_t(1) << 40)) return "data too large";
+
+  DeviceGeometry& g = p->g;
+  g.kind = proj->kind;
+  g.nz = int(vol->shape[0]);
+  g.ny = int(vol->shape[1]);
+  g.nx = int(vol->shape[2]);
+  g.oz = g.nz / 2;
+  g.oy = g.ny / 2;
+  g.ox = g.nx / 2;
+  g.rows = int(proj->det_shape[0]);
+  g.cols = int(proj->det_shape[1]);
+  g.nangles = int(proj->num_angles);
+  g.ov = g.rows / 2;
+  g.ou = g.cols / 2;
+  g.det_ss = det_ss;
+  g.vox_ss = voxel_ss;
+  const int shape[3] = {g.nz, g.ny, g.nx};
+  const int anchor[3] = {g.oz, g.oy, g.ox};
+  V3 vs, origin;
+  for (int i = 0; i < 3; ++i) {
+    vs[i] = vol->size[i] / double(vol->shape[i]);
+    g.vs[i] = float(vs[i]);
+    // world position of the anchor voxel's centre
+    origin[i] = vol->pos[i] - 0.5 * vol->size[i] + (anchor[i] + 0.5) * vs[i];
+  }
+  const double vox_volume = vs[0] * vs[1] * vs[2];
+  const bool cone = proj->kind == TSGB_CONE;
+
+  p->host_params.assign(g.nangles, AngleParams{});
+  p->layouts.clear();
+  columns->assign(size_t(g.nangles) * g.cols, ColumnEntry{});
+  sep_angles->clear();
+  gen_angles->clear();
+
+  for (int t = 0; t < g.nangles; ++t) {
+    const double* row = proj->vectors + 12 * size_t(t);
+    V3 src_w{{row[0], row[1], row[2]}}, det_w{{row[3], row[4], row[5]}};
+    V3 v_w{{row[6], row[7], row[8]}}, u_w{{row[9], row[10], row[11]}};
+    if (!finite3(src_w) || !finite3(det_w) || !finite3(v_w) || !finite3(u_w))
+      return "non-finite geometry vector at angle " + std::to_string(t);
+    if (norm(u_w) == 0.0 || norm(v_w) == 0.0 || norm(cross(u_w, v_w)) == 0.0)
+      return "degenerate detector pixel vectors at angle " + std::to_string(t);
+
+    // Anchored pixel origin: centre of pixel (ov, ou) (world units).
+    V3 dc_w = axpy(axpy(det_w, g.ov + 0.5 - 0.5 * g.rows, v_w), g.ou + 0.5 - 0.5 * g.cols, u_w);
+    // To anchored voxel coordinates.
+    V3 U, V, Dc, S, R;
+    for (int i = 0; i < 3; ++i) {
+      U[i] = u_w[i] / vs[i];
+      V[i] = v_w[i] / vs[i];
+      Dc[i] = (dc_w[i] - origin[i]) / vs[i];
+      S[i] = (src_w[i] - origin[i]) / vs[i];  // source (cone)
+      R[i] = src_w[i] / vs[i];                // ray direction (parallel)
+    }
+    V3 ref;  // central ray direction in voxel units
+    if (cone) {
+      for (int i = 0; i < 3; ++i) ref[i] = (det_w[i] - src_w[i]) / vs[i];
+    } else {
+      ref = R;
+    }
+    if (norm(ref) == 0.0) return "zero ray direction at angle " + std::to_string(t);
+
+    AngleParams& ap = p->host_params[t];
+    const int d = argmax_abs(ref, -1);
+    const int b = argmax_abs(V, d);
+    const int a = 3 - d - b;
+    ap.d = d;
+    ap.a = a;
+    ap.b = b;
+    const double vn = norm(V);
+    const bool separable = det_ss == 1 && std::fabs(V[d]) <= 1e-12 * vn && std::fabs(V[a]) <= 1e-12 * vn;
+    if (separable) {
+      V[d] = 0.0;
+      V[a] = 0.0;
+    }
+    ap.separable = separable ? 1 : 0;
+
+    // Ray coefficients over (1, ut, vt).
+    double e[3], ca[3], ma[3], cb[3], mb[3];
+    if (cone) {
+      V3 D = sub(Dc, S);
+      if (D[d] == 0.0) return "detector centre lies in the source's dominant plane";
+      const double sc = 1.0 / D[d];  // normalise so den = 1 at the anchored pixel
+      const double ed[3] = {D[d], U[d], V[d]};
+      const double ea[3] = {D[a], U[a], V[a]};
+      const double eb[3] = {D[b], U[b], V[b]};
+      for (int j = 0; j < 3; ++j) {
+        e[j] = ed[j] * sc;
+        ca[j] = (S[a] * ed[j] - S[d] * ea[j]) * sc;
+        ma[j] = ea[j] * sc;
+        cb[j] = (S[b] * ed[j] - S[d] * eb[j]) * sc;
+        mb[j] = eb[j] * sc;
+      }
+    } else {
+      if (R[d] == 0.0) return "ray parallel to every volume plane";
+      const double sa = R[a] / R[d], sb = R[b] / R[d];
+      e[0] = 1.0;
+      e[1] = e[2] = 0.0;
+      ca[0] = Dc[a] - Dc[d] * sa;
+      ca[1] = U[a] - U[d] * sa;
+      ca[2] = V[a] - V[d] * sa;
+      cb[0] = Dc[b] - Dc[d] * sb;
+      cb[1] = U[b] - U[d] * sb;
+      cb[2] = V[b] - V[d] * sb;
+      ma[0] = sa;
+      mb[0] = sb;
+      ma[1] = ma[2] = mb[1] = mb[2] = 0.0;
+    }
+    for (int j = 0; j < 3; ++j) {
+      ap.e[j] = float(e[j]);
+      ap.ca[j] = float(ca[j]);
+      ap.ma[j] = float(ma[j]);
+      ap.cb[j] = float(cb[j]);
+      ap.mb[j] = float(mb[j]);
+    }
+
+    // Voxel -> detector projection, anchored coordinates in (z, y, x) order.
+    double pu[4], pv[4], pw[4];
+    if (cone) {
+      V3 r = sub(Dc, S);
+      V3 nu = cross(V, r), nv = cross(r, U), nw = cross(U, V);
+      const double den0 = -dot(S, nw);
+      if (den0 == 0.0) return "source lies in the detector plane's parallel through the volume";
+      for (int i = 0; i < 3; ++i) {
+        pu[i] = nu[i] / den0;
+        pv[i] = nv[i] / den0;
+        pw[i] = nw[i] / den0;
+      }
+      pu[3] = -dot(S, nu) / den0;
+      pv[3] = -dot(S, nv) / den0;
+      pw[3] = 1.0;
+      // Bilinear weight: K^2 / |den0|^3 * |P - S|_world / dn^3 (see header).
+      const double K = dot(r, nw);
+      ap.bil_scale = float(K * K / std::fabs(den0 * den0 * den0));
+    } else {
+      V3 rv = cross(R, V), ur = cross(U, R);
+      const double den = dot(R, cross(U, V));
+      if (den == 0.0) return "ray direction lies in the detector plane";
+      for (int i = 0; i < 3; ++i) {
+        pu[i] = -rv[i] / den;
+        pv[i] = -ur[i] / den;
+        pw[i] = 0.0;
+      }
+      pu[3] = dot(Dc, rv) / den;
+      pv[3] = dot(Dc, ur) / den;
+      pw[3] = 1.0;
+      V3 nw_w = cross(u_w, v_w);
+      ap.bil_scale = float(vox_volume * norm(src_w) / std::fabs(dot(src_w, nw_w)));
+    }
+    for (int i = 0; i < 4; ++i) {
+      ap.pu[i] = float(pu[i]);
+      ap.pv[i] = float(pv[i]);
+      ap.pw[i] = float(pw[i]);
+    }
+    for (int i = 0; i < 3; ++i) ap.src[i] = float(S[i]);
+
+    // Forward-projection volume copy for this (d, a, b).
+    int li = -1;
+    for (size_t l = 0; l < p->layouts.size(); ++l)
+      if (p->layouts[l].d == d && p->layouts[l].a == a && p->layouts[l].b == b) li = int(l);
+    if (li < 0) {
+      Layout L;
+      L.d = d;
+      L.a = a;
+      L.b = b;
+      L.n_d = shape[d];
+      L.n_a = shape[a];
+      L.n_b = shape[b];
+      L.offset_floats = 0;
+      p->layouts.push_back(L);
+      li = int(p->layouts.size()) - 1;
+    }
+    ap.layout = li;
+
+    // Column table (separable angles).
+    if (separable) {
+      for (int iu = 0; iu < g.cols; ++iu) {
+        const double ut = double(iu - g.ou);
+        const double den = e[0] + e[1] * ut;
+        ColumnEntry& c = (*columns)[size_t(t) * g.cols + iu];
+        c.Xa = float((ca[0] + ca[1] * ut) / den);
+        c.ma = float((ma[0] + ma[1] * ut) / den);
+        c.P = float((cb[0] + cb[1] * ut) / den);
+        c.Q = float((mb[0] + mb[1] * ut) / den);
+        c.R = float(cb[2] / den);
+        c.S = float(mb[2] / den);
+      }
+    }
+    ap.bp_general = (separable && b == 0) ? 0 : 1;
+    if (ap.bp_general)
+      gen_angles->push_back(t);
+    else
+      sep_angles->push_back(t);
+  }
+
+  int64_t off = 0;
+  for (auto& L : p->layouts) {
+    L.offset_floats = off;
+    off += (L.floats() + 63) / 64 * 64;  // keep every copy 256-byte aligned
+  }
+  for (auto& ap : p->host_params) {
+    const Layout& L = p->layouts[ap.layout];
+    ap.ws_offset = L.offset_floats;
+    ap.n_d = int(L.n_d);
+    ap.n_a = int(L.n_a);
+    ap.n_b = int(L.n_b);
+    ap.o_d = anchor[L.d];
+    ap.o_a = anchor[L.a];
+    ap.o_b = anchor[L.b];
+    ap.stride_d = int(L.n_a + 2 * kPad);
+    ap.stride_b = int(L.n_d * (L.n_a + 2 * kPad));
+    ap.vs_d = float(vs[L.d]);
+    ap.vs_a = float(vs[L.a]);
+    ap.vs_b = float(vs[L.b]);
+  }
+  p->fp_workspace_floats = off;
+  p->n_general_bp = int(gen_angles->size());
+  p->n_separable_bp = int(sep_angles->size());
+  return std::string();
+}
+
+}  // namespace tsgb

@@ -1,0 +1,122 @@
+// Internal types of the tomosipo_gb300 projector (not part of the C ABI).
+//
+// Coordinates. Kernels work in "anchored voxel coordinates": one unit per
+// voxel along each axis, origin at the centre of voxel o = N / 2 (integer
+// division), so voxel i sits at the integer i - o. Keeping the origin inside
+// the volume keeps fp32 positions small (|q| <= N/2), which is what bounds
+// their rounding error. Detector pixels are anchored the same way:
+// pixel iu sits at iu - o_u with o_u = cols / 2.
+//
+// Discretisation (forward projection, Joseph's method). For each angle the
+// host picks a dominant volume axis d (largest component of the central ray
+// in voxel units) and two in-plane axes a and b. A ray is sampled on every
+// voxel-centre plane k of axis d; its in-plane position there is
+//   q_a(k) = X_a + kt * m_a,   q_b(k) = X_b + kt * m_b,   kt = k - o_d,
+// where X is the ray's hit point on plane kt = 0 and m its slope per plane.
+// The sample is the bilinear interpolation of the four voxels around
+// (q_a, q_b) with zeros outside the volume. The ray sum is scaled by the
+// world-space step between planes, W = |(vs_d, vs_a m_a, vs_b m_b)|.
+// The matched backprojection is the exact transpose of this.
+#pragma once
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "tomosipo_gb300.h"
+
+namespace tsgb {
+
+constexpr int kPad = 2;        // zero padding of the forward-projection volume copies
+constexpr int kMaxLayouts = 6; // axis permutations (d, a, b)
+
+// Per-angle parameters, read uniformly by all threads of a block.
+struct alignas(16) AngleParams {
+  int d, a, b;       // volume axes (0 = z, 1 = y, 2 = x)
+  int separable;     // det_v has no d or a component: column table is valid
+  int layout;        // index of the padded volume copy used by the forward projector
+  int bp_general;    // 1: backprojected by the general kernel (else separable kernel)
+  int pad0, pad1;
+  // Ray coefficients, functions of anchored pixel coordinates (ut, vt):
+  //   den = e0 + e1 ut + e2 vt,  X_a = (ca . [1,ut,vt]) / den,  m_a = (ma . [1,ut,vt]) / den
+  // and the same for b. Parallel beams have den = 1.
+  float e[4], ca[4], ma[4], cb[4], mb[4];
+  // Projection of an anchored voxel position P = (z, y, x) onto the detector:
+  //   ut = (pu . [P,1]) / (pw . [P,1]),  vt = (pv . [P,1]) / (pw . [P,1]),
+  // normalised so that pw . [0,1] = 1.
+  float pu[4], pv[4], pw[4];
+  // Bilinear backprojection weight: parallel: bil_scale;
+  // cone: bil_scale * |P - src|_world / (pw . [P,1])^3.
+  float bil_scale;
+  float src[3];      // source in anchored voxel coordinates (cone)
+  // Addressing of this angle's padded forward-projection copy: element
+  // (k along d, i along a, j along b; unpadded indices) is at
+  //   ws_offset + (j + kPad) * stride_b + k * stride_d + (i + kPad).
+  long long ws_offset;
+  int n_d, n_a, n_b;
+  int o_d, o_a, o_b;
+  int stride_d, stride_b;
+  float vs_d, vs_a, vs_b;  // voxel size along d, a, b (world units)
+  float pad2;
+};
+
+// Column table entry for separable angles, one per (angle, detector column):
+//   q_a(kt) = X_a + kt m_a
+//   q_b(kt, vt) = (P + vt R) + kt (Q + vt S)
+struct alignas(16) ColumnEntry {
+  float Xa, ma, P, Q;
+  float R, S, pad0, pad1;
+};
+
+struct Layout {
+  int d, a, b;
+  int64_t n_d, n_a, n_b;   // unpadded extents
+  int64_t offset_floats;   // offset of this copy in the forward workspace
+  int64_t floats() const { return (n_b + 2 * kPad) * n_d * (n_a + 2 * kPad); }
+};
+
+struct DeviceGeometry {
+  int kind;                 // TSGB_PARALLEL / TSGB_CONE
+  int nz, ny, nx;           // volume shape
+  int oz, oy, ox;           // voxel anchors (N / 2)
+  int rows, cols, nangles;  // sinogram shape
+  int ov, ou;               // pixel anchors
+  float vs[3];              // voxel size (z, y, x), world units
+  int det_ss, vox_ss;       // supersampling factors
+};
+
+}  // namespace tsgb
+
+struct tsgb_projector {
+  int device;
+  tsgb::DeviceGeometry g;
+  std::vector<tsgb::AngleParams> host_params;
+  std::vector<tsgb::Layout> layouts;
+  int64_t fp_workspace_floats = 0;
+  int n_general_bp = 0;         // angles handled by the general BP kernel
+  int n_separable_bp = 0;       // angles handled by the separable BP kernel
+  tsgb::AngleParams* d_params = nullptr;
+  tsgb::ColumnEntry* d_columns = nullptr;  // [nangles][cols]
+  int* d_sep_angles = nullptr;             // angle ids for the separable BP kernel
+  int* d_gen_angles = nullptr;             // angle ids for the general BP kernel
+};
+
+namespace tsgb {
+
+// Host-side construction of the per-angle tables in fp64 (plan.cpp). Fills
+// p->g, p->host_params, p->layouts and the column table; returns an empty
+// string on success, else the error message.
+std::string build_plan(const tsgb_volume_desc* vol, const tsgb_projection_desc* proj,
+                       int voxel_ss, int det_ss, tsgb_projector* p,
+                       std::vector<ColumnEntry>* columns,
+                       std::vector<int>* sep_angles, std::vector<int>* gen_angles);
+
+// Kernel launchers (fp.cu, bp.cu). All return cudaGetLastError() as int.
+int launch_fp(const tsgb_projector* p, const float* vol, float* sino, bool additive,
+              float* workspace, void* stream);
+int launch_bp_matched(const tsgb_projector* p, float* vol, const float* sino, bool additive,
+                      float* workspace, void* stream);
+int launch_bp_bilinear(const tsgb_projector* p, float* vol, const float* sino, bool additive,
+                       void* stream);
+
+}  // namespace tsgb

@@ -1,0 +1,7 @@
+from .base import link, geometry_shape, are_compatible, Link, backends
+from .numpy import NumpyLink
+
+try:
+    from .torch import TorchLink
+except ImportError:  # torch missing: NumPy links only
+    TorchLink = None

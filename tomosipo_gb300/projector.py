@@ -1,0 +1,185 @@
+"""GB300 link layer: replaces tomosipo's ``tomosipo/astra.py`` (lines 80-217).
+
+``create_projector`` plays the role of ``create_astra_projector``
+(``astra.py:80-98``) and ``direct_fp`` / ``direct_bp`` the role of the
+functions that call ``astra.experimental.direct_FPBP3D`` (``astra.py:104-217``),
+with the same argument meaning and the same ``ValueError`` on device mismatch.
+Work runs on the current CUDA stream of the data's device, asynchronously.
+Host (NumPy / CPU tensor) data are staged through the current CUDA device;
+without a CUDA device every projection raises ``RuntimeError``.
+"""
+import ctypes
+
+import numpy as np
+import torch
+
+from . import _native
+from .geometry import VolumeGeometry, is_volume
+from .links.base import are_compatible
+
+BP_KINDS = {"matched": _native.TSGB_BP_MATCHED, "bilinear": _native.TSGB_BP_BILINEAR}
+
+
+def projection_vectors(pg):
+    """(kind, rows, cols, vectors[num_angles, 12]) of a projection geometry.
+
+    Row layout: [src_pos or ray_dir, det_pos, det_v, det_u], each (z, y, x).
+    """
+    v = pg.to_vec()
+    first = v.src_pos if pg.is_cone else v.ray_dir
+    vec = np.concatenate([first, v.det_pos, v.det_v, v.det_u], axis=1)
+    kind = _native.TSGB_CONE if pg.is_cone else _native.TSGB_PARALLEL
+    rows, cols = v.det_shape
+    return kind, rows, cols, np.ascontiguousarray(vec, dtype=np.float64)
+
+
+class Projector:
+    """Geometry of one (volume, projection) pair plus its native handles.
+
+    Native projectors are created lazily, one per CUDA device, and freed with
+    this object (ASTRA projector ids in the reference are never freed).
+    """
+
+    def __init__(self, vg, pg, voxel_supersampling=1, detector_supersampling=1):
+        if not isinstance(vg, VolumeGeometry):
+            raise TypeError(f"Expected an axis-aligned VolumeGeometry. Got {type(vg)}.")
+        self.vg = vg
+        self.pg = pg
+        self.voxel_supersampling = int(voxel_supersampling)
+        self.detector_supersampling = int(detector_supersampling)
+        kind, rows, cols, vec = projection_vectors(pg)
+        self._vectors = vec  # kept alive: the descriptor points into it
+        self.vol_desc = _native.VolumeDesc()
+        self.vol_desc.shape[:] = list(vg.shape)
+        self.vol_desc.pos[:] = [float(x) for x in vg.pos[0]]
+        self.vol_desc.size[:] = [float(x) for x in vg.size]
+        self.proj_desc = _native.ProjectionDesc()
+        self.proj_desc.kind = kind
+        self.proj_desc.det_shape[:] = [rows, cols]
+        self.proj_desc.num_angles = vec.shape[0]
+        self.proj_desc.vectors = vec.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+        self.vol_shape = tuple(vg.shape)
+        self.sino_shape = (rows, vec.shape[0], cols)
+        self._handles = {}
+
+    def handle(self, device_index):
+        h = self._handles.get(device_index)
+        if h is None:
+            lib = _native.load()
+            out = ctypes.c_void_p()
+            with torch.cuda.device(device_index):
+                rc = lib.tsgb_projector_create(
+                    ctypes.byref(self.vol_desc),
+                    ctypes.byref(self.proj_desc),
+                    self.voxel_supersampling,
+                    self.detector_supersampling,
+                    ctypes.byref(out),
+                )
+            _native.check(rc, "tsgb_projector_create")
+            h = out.value
+            self._handles[device_index] = h
+        return h
+
+    def workspace_bytes(self, device_index, forward, bp_kind="matched"):
+        lib = _native.load()
+        h = self.handle(device_index)
+        if forward:
+            return int(lib.tsgb_fp_workspace_bytes(h))
+        return int(lib.tsgb_bp_workspace_bytes(h, BP_KINDS[bp_kind]))
+
+    def __del__(self):
+        handles, self._handles = getattr(self, "_handles", {}), {}
+        if handles and _native._lib is not None:
+            for h in handles.values():
+                try:
+                    _native._lib.tsgb_projector_destroy(h)
+                except Exception:
+                    pass
+
+
+def create_projector(volume_geometry, projection_geometry, *, voxel_supersampling=1,
+                     detector_supersampling=1):
+    """Projector for an axis-aligned volume and any projection geometry."""
+    if not is_volume(volume_geometry) or not isinstance(volume_geometry, VolumeGeometry):
+        raise TypeError("create_projector expects an axis-aligned VolumeGeometry")
+    if voxel_supersampling < 1 or detector_supersampling < 1:
+        raise ValueError("supersampling factors must be >= 1")
+    return Projector(volume_geometry, projection_geometry, voxel_supersampling,
+                     detector_supersampling)
+
+
+# tomosipo name for the same function (tomosipo/astra.py:80)
+create_astra_projector = create_projector
+
+
+def _cuda_device_for_host_data():
+    if not torch.cuda.is_available():
+        raise RuntimeError(
+            "tomosipo_gb300 projects on a CUDA GPU only; no CUDA device is available "
+            "(there is no CPU fallback)."
+        )
+    return torch.device("cuda", torch.cuda.current_device())
+
+
+def _as_device_tensor(arr, device, copy_in):
+    """Device tensor view of a link's data; returns (tensor, needs_copy_back)."""
+    if isinstance(arr, torch.Tensor) and arr.is_cuda:
+        return arr, False
+    t = torch.from_numpy(arr) if isinstance(arr, np.ndarray) else arr
+    if copy_in:
+        return t.to(device, non_blocking=False), True
+    return torch.empty(t.shape, dtype=torch.float32, device=device), True
+
+
+def direct_project(projector, vol_link, proj_link, forward=None, additive=False,
+                   bp_kind="matched"):
+    """Forward (``forward=True``) or back project between two links."""
+    if forward is None:
+        raise ValueError("project must be given a forward argument (True/False).")
+    if bp_kind not in BP_KINDS:
+        raise ValueError(f"bp_kind must be one of {sorted(BP_KINDS)}. Got {bp_kind!r}.")
+    if not are_compatible(vol_link, proj_link):
+        raise ValueError(
+            "Cannot perform projection on volume and projection data, because they are "
+            "not compatible. Usually, this indicates that the data are located on "
+            "different computing devices. "
+        )
+    if tuple(vol_link.shape) != projector.vol_shape or tuple(proj_link.shape) != projector.sino_shape:
+        raise ValueError(
+            f"Expected volume {projector.vol_shape} and sinogram {projector.sino_shape}. "
+            f"Got {tuple(vol_link.shape)} and {tuple(proj_link.shape)}."
+        )
+    vol, sino = vol_link.data, proj_link.data
+    on_gpu = isinstance(vol, torch.Tensor) and vol.is_cuda
+    device = vol.device if on_gpu else _cuda_device_for_host_data()
+    src, dst = (vol, sino) if forward else (sino, vol)
+    d_src, _ = _as_device_tensor(src, device, copy_in=True)
+    d_dst, copy_back = _as_device_tensor(dst, device, copy_in=additive)
+    lib = _native.load()
+    with torch.cuda.device(device):
+        h = projector.handle(device.index)
+        stream = torch.cuda.current_stream(device).cuda_stream
+        nbytes = projector.workspace_bytes(device.index, forward, bp_kind)
+        ws = torch.empty(max(nbytes, 1), dtype=torch.uint8, device=device)
+        if forward:
+            rc = lib.tsgb_direct_fp(h, d_src.data_ptr(), d_dst.data_ptr(), int(bool(additive)),
+                                    ws.data_ptr(), nbytes, stream)
+        else:
+            rc = lib.tsgb_direct_bp(h, d_dst.data_ptr(), d_src.data_ptr(), int(bool(additive)),
+                                    BP_KINDS[bp_kind], ws.data_ptr(), nbytes, stream)
+        _native.check(rc, "tsgb_direct_fp" if forward else "tsgb_direct_bp")
+    if copy_back:
+        host = d_dst.cpu()
+        if isinstance(dst, np.ndarray):
+            np.copyto(dst, host.numpy())
+        else:
+            dst.copy_(host)
+
+
+def direct_fp(projector, vol_data, proj_data, additive=False):
+    return direct_project(projector, vol_data, proj_data, forward=True, additive=additive)
+
+
+def direct_bp(projector, vol_data, proj_data, additive=False, bp_kind="matched"):
+    return direct_project(projector, vol_data, proj_data, forward=False, additive=additive,
+                          bp_kind=bp_kind)
