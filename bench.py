@@ -1,0 +1,432 @@
+"""Headline benchmark: cone FP+BP GUPS at 512^3 / 1024 angles on GB300.
+
+One step = one forward projection A(x) and one matched backprojection A.T(y)
+of the cone-beam workload (volume 512^3 on the unit cube, ts.cone(size=sqrt2,
+cone_angle=0.5), 1024 angles over 2 pi, detector 512 x 768), with inputs
+resident in HBM. GUPS = (U_FP + U_BP) / time / 1e9 with U = 512^3 * 1024
+voxel-angle updates per projection.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Under torchrun (N > 1) every rank runs the same workload on its own GPU
+(independent replicas, no collective on the data path; weak scaling) and rank
+0 prints one JSON line with the whole-job value (all ranks' updates over the
+slowest rank's time).
+
+``--impl reference`` times the reference implementation of this path on the
+host cores. The reference (tomosipo) is pure Python around ASTRA's GPU
+projector and has no CPU implementation of its own, and ASTRA is not
+installed, so that arm runs the project's FP64 CPU oracle (oracle/) with all
+host threads on a bounded sample of the same workload.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+METRIC = "cone FP+BP GUPS at 512^3/1024 angles"
+# Workloads: the headline one (the metric's) and a small one of the same
+# geometry family for profiler captures (volume 256^3, 360 angles, 256x384).
+WORKLOADS = {"headline": (512, 1024, (512, 768)), "c2": (256, 360, (256, 384))}
+N, ANGLES, DET = WORKLOADS["headline"]
+HBM_FALLBACK_GBS = 6800.0
+BYTES_PER_UPDATE = 4  # one fp32 voxel operand per voxel-angle update
+
+
+def metric_name():
+    """The headline metric; the c2 profiling workload names its own size."""
+    return METRIC if (N, ANGLES) == (512, 1024) else f"cone FP+BP GUPS at {N}^3/{ANGLES} angles"
+
+
+def workload_geometry(ts):
+    vg = ts.volume(shape=N, size=1)
+    pg = ts.cone(angles=ANGLES, shape=DET, size=np.sqrt(2), cone_angle=0.5)
+    return vg, pg
+
+
+def config(extra=None):
+    c = {
+        "workload": f"cone FP+BP, volume {N}^3 unit cube, ts.cone(size=sqrt2, cone_angle=0.5), "
+        f"{ANGLES} angles over 2pi, detector {DET[0]}x{DET[1]}, fp32, matched (exact-transpose) BP",
+        "volume": [N, N, N],
+        "angles": ANGLES,
+        "detector": list(DET),
+        "phantom": "20 seeded random ellipsoids, densities U[0.1,1] (seed 2)",
+        "l2": f"inputs larger than L2 (volume {4 * N ** 3 / 1e9:.2f} GB, sinogram "
+        f"{4 * DET[0] * DET[1] * ANGLES / 1e9:.2f} GB; L2 129 MB)",
+    }
+    if extra:
+        c.update(extra)
+    return c
+
+
+def measured_peak_hbm():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return HBM_FALLBACK_GBS, "fallback"
+
+
+# --------------------------------------------------------------------------- clocks
+class ClockSampler:
+    """nvidia-smi clock / throttle-reason samples every 200 ms while running."""
+
+    FIELDS = (
+        "index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+        "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+        "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap"
+    )
+
+    def __init__(self, gpu_index):
+        self.gpu_index = gpu_index
+        self.proc = None
+        self.lines = []
+        self._thread = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.gpu_index}", f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True,
+            )
+        except OSError:
+            self.proc = None
+            return
+        self._thread = threading.Thread(target=self._read, daemon=True)
+        self._thread.start()
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        if self._thread:
+            self._thread.join(timeout=2)
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.lines:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for name, val in zip(names, parts[5:9]):
+                if val.lower() == "active":
+                    reasons.add(name)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        return {
+            "sm_mhz": statistics.median(sm),
+            "sm_max_mhz": max(smax),
+            "reasons": sorted(reasons),
+            "samples": len(sm),
+        }
+
+
+# --------------------------------------------------------------------------- CPU baseline
+def cpu_baseline_sample(threads=None, angles=None):
+    """Time the FP64 oracle (FP + matched BP) on a subset of the workload's angles.
+
+    Returns (GUPS, dict) for the updates processed: 512^3 * n_angles per projection.
+    """
+    import tomosipo_gb300 as ts
+    from oracle import oracle as orc
+
+    threads = threads or (os.cpu_count() or 1)
+    # one angle per thread, at least 8: about 10-20 s of CPU work
+    n_angles = angles or max(8, min(threads, 32))
+    sub = pg[:: ANGLES // n_angles][:n_angles]
+    rng = np.random.default_rng(2)
+    x = rng.random(vg.shape)
+    t0 = time.perf_counter()
+    y = orc.fp(vg, sub, x, threads=threads)
+    t1 = time.perf_counter()
+    orc.bp_matched(vg, sub, y, threads=threads)
+    t2 = time.perf_counter()
+    updates = 2 * N ** 3 * sub.num_angles
+    gups = updates / (t2 - t0) / 1e9
+    return gups, {
+        "cores": threads,
+        "sample": f"FP + matched BP of {sub.num_angles} of the {ANGLES} angles (every "
+        f"{ANGLES // n_angles}th) at full {N}^3 / {DET[0]}x{DET[1]} size; fp64 oracle; "
+        f"FP {t1 - t0:.2f} s, BP {t2 - t1:.2f} s",
+    }
+
+
+def run_reference(args, rank, world):
+    if rank != 0:
+        return 0
+    from tomosipo_gb300._build import build_oracle
+
+    build_oracle()
+    vals = []
+    info = None
+    for _ in range(max(0, args.warmup_ref)):
+        cpu_baseline_sample()
+    for _ in range(args.steps_ref):
+        v, info = cpu_baseline_sample()
+        vals.append(v)
+    value = statistics.median(vals)
+    line = {
+        "impl": "reference",
+        "metric": metric_name(),
+        "value": value,
+        "unit": "GUPS",
+        "n_gpus": 0,
+        "steps": args.steps_ref,
+        "warmup": args.warmup_ref,
+        "higher_is_better": True,
+        "dtype": "f64",
+        "data": "synthetic",
+        "config": config({"arm": "reference CPU path: FP64 oracle (tomosipo has no CPU "
+                          "projector; ASTRA not installable offline)"}),
+        "cpu_baseline": {"value": value, "unit": "GUPS", "cores": info["cores"],
+                         "kind": "port", "sample": info["sample"]},
+        "e2e": {"value": value, "unit": "GUPS", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "vs_baseline": None,
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+# --------------------------------------------------------------------------- GPU arm
+def ellipsoid_phantom_gpu(torch, device, n=20, seed=2):
+    """Sum of ``n`` seeded random ellipsoids (densities U[0.1, 1]) on [-1, 1]^3."""
+    g = torch.Generator(device="cpu").manual_seed(seed)
+    ax = torch.linspace(-1, 1, N, device=device)
+    yy, xx = ax[None, :, None], ax[None, None, :]
+    x = torch.zeros((N, N, N), device=device)
+    params = []
+    for _ in range(n):
+        c = (torch.rand(3, generator=g) - 0.5).tolist()
+        r = (torch.rand(3, generator=g) * 0.35 + 0.1).tolist()
+        rho = float(torch.rand(1, generator=g)) * 0.9 + 0.1
+        params.append((c, r, rho))
+    for z0 in range(0, N, 64):  # z slabs keep temporaries small
+        zz = ax[z0:z0 + 64, None, None]
+        for c, r, rho in params:
+            m = ((zz - c[0]) / r[0]) ** 2 + ((yy - c[1]) / r[1]) ** 2 + ((xx - c[2]) / r[2]) ** 2
+            x[z0:z0 + 64] += rho * (m <= 1)
+    return x
+
+
+def run_ours(args, rank, world, local_rank):
+    import torch
+    import torch.distributed as dist
+
+    import __graft_entry__
+
+    __graft_entry__.build()
+    import tomosipo_gb300 as ts
+
+    device = torch.device("cuda", local_rank)
+    torch.cuda.set_device(device)
+    vg, pg = workload_geometry(ts)
+    A = ts.operator(vg, pg)
+    x = ellipsoid_phantom_gpu(torch, device)
+    y = torch.empty(A.range_shape, device=device)
+    v = torch.empty(A.domain_shape, device=device)
+    stats = A.projector.stats(device.index)
+    U = N ** 3 * ANGLES
+
+    def barrier():
+        if world > 1:
+            dist.barrier()
+
+    def step():
+        A(x, out=y)
+        A.T(y, out=v)
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+
+    stream = torch.cuda.current_stream(device)
+    ev = [[torch.cuda.Event(enable_timing=True) for _ in range(3)] for _ in range(args.steps)]
+    clocks = ClockSampler(local_rank)
+    barrier()
+    torch.cuda.synchronize()
+    clocks.start()
+    t_start = torch.cuda.Event(enable_timing=True)
+    t_end = torch.cuda.Event(enable_timing=True)
+    t_start.record(stream)
+    for i in range(args.steps):
+        ev[i][0].record(stream)
+        A(x, out=y)
+        ev[i][1].record(stream)
+        A.T(y, out=v)
+        ev[i][2].record(stream)
+    t_end.record(stream)
+    torch.cuda.synchronize()
+    barrier()
+    clock_info = clocks.stop()
+    total_ms = t_start.elapsed_time(t_end)
+    fp_ms = [e[0].elapsed_time(e[1]) for e in ev]
+    bp_ms = [e[1].elapsed_time(e[2]) for e in ev]
+
+    if world > 1:
+        t = torch.tensor([total_ms], device=device)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_ms = float(t.item())
+    ms_per_step = total_ms / args.steps
+    value = world * 2 * U * args.steps / (total_ms / 1e3) / 1e9
+
+    # End to end through the public API with pinned host buffers: every step
+    # copies the volume in, projects, copies the sinogram out, copies it back
+    # in, backprojects and copies the volume out (A(x_host), A.T(y_host)).
+    e2e = None
+    if not args.no_e2e:
+        xh = x.cpu().pin_memory()
+        yh = torch.empty(A.range_shape, dtype=torch.float32).pin_memory()
+        vh = torch.empty(A.domain_shape, dtype=torch.float32).pin_memory()
+        for _ in range(max(1, args.warmup // 2)):
+            A(xh, out=yh)
+            A.T(yh, out=vh)
+        torch.cuda.synchronize()
+        barrier()
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            A(xh, out=yh)
+            A.T(yh, out=vh)
+        torch.cuda.synchronize()
+        dt = time.perf_counter() - t0
+        if world > 1:
+            t = torch.tensor([dt], device=device)
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            dt = float(t.item())
+        barrier()
+        vol_b = 4 * N ** 3
+        sino_b = 4 * DET[0] * DET[1] * ANGLES
+        e2e = {
+            "value": world * 2 * U * args.steps / dt / 1e9,
+            "unit": "GUPS",
+            "h2d_bytes_per_step": vol_b + sino_b,
+            "d2h_bytes_per_step": sino_b + vol_b,
+            "ms_per_step": 1e3 * dt / args.steps,
+            "path": "ts.operator A(x_host)->y_host, A.T(y_host)->x_host, pinned buffers",
+        }
+
+    if rank != 0:
+        return 0
+
+    peak, peak_kind = measured_peak_hbm()
+    bp_avg = statistics.mean(bp_ms) / 1e3
+    fp_avg = statistics.mean(fp_ms) / 1e3
+    dom_name, dom_t = ("bp_matched (weight pass + separable gather)", bp_avg)
+    if fp_avg > bp_avg:
+        dom_name, dom_t = ("fp (layout copies + ray kernel)", fp_avg)
+    achieved = BYTES_PER_UPDATE * U / dom_t / 1e9
+    traffic = None
+    tpath = os.path.join(ROOT, "profiles", "traffic.json")
+    if os.path.exists(tpath):
+        try:
+            with open(tpath) as f:
+                traffic = json.load(f).get("bp_matched_bytes_per_launch_512")
+        except (OSError, ValueError):
+            traffic = None
+    cpu = None
+    if world == 1 and not args.no_cpu_baseline:
+        gups, info = cpu_baseline_sample()
+        cpu = {"value": gups, "unit": "GUPS", "cores": info["cores"], "kind": "port",
+               "sample": info["sample"]}
+    line = {
+        "metric": metric_name(),
+        "value": value,
+        "unit": "GUPS",
+        "n_gpus": world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": ms_per_step,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f32",
+        "data": "synthetic",
+        "config": config({"parallelism": f"replicas x{world}" if world > 1 else "single GPU"}),
+        "fp_ms": statistics.mean(fp_ms),
+        "bp_ms": statistics.mean(bp_ms),
+        "roofline": {
+            "bound": "hbm",
+            "kernel": dom_name,
+            "achieved": achieved,
+            "peak": peak,
+            "unit": "GB/s",
+            "frac": achieved / peak,
+            "peak_kind": peak_kind,
+            "traffic": traffic,
+            "algorithmic_bytes": f"{BYTES_PER_UPDATE} B per voxel-angle update x {N}^3 x {ANGLES}",
+            "step_frac": BYTES_PER_UPDATE * value * 1e9 / world / peak / 1e9,
+        },
+        "cpu_baseline": cpu,
+        "e2e": e2e,
+        "gpu_launches": args.steps * (stats["fp_launches"] + stats["bp_matched_launches"]),
+        "clocks": clock_info,
+        "plan": stats,
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def main():
+    p = argparse.ArgumentParser(description=__doc__.split("\n")[0])
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=5)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    p.add_argument("--no-e2e", action="store_true")
+    p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--workload", choices=sorted(WORKLOADS), default="headline",
+                   help="headline = the metric's 512^3/1024 workload; c2 = 256^3/360 (profiling)")
+    args = p.parse_args()
+    global N, ANGLES, DET
+    N, ANGLES, DET = WORKLOADS[args.workload]
+    args.steps_ref = max(1, min(args.steps, 2))
+    args.warmup_ref = 0
+    if args.warmup < 3 and args.impl == "ours":
+        print("warning: fewer than 3 warm-up steps", file=sys.stderr)
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+    if args.impl == "reference":
+        return run_reference(args, rank, world)
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+
+        torch.cuda.set_device(local_rank)
+        dist.init_process_group("nccl")
+    try:
+        return run_ours(args, rank, world, local_rank)
+    finally:
+        if world > 1:
+            import torch.distributed as dist
+
+            dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    sys.exit(main())

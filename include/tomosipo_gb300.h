@@ -97,6 +97,17 @@ int tsgb_direct_bp(tsgb_projector* p, float* vol, const float* sino,
 int tsgb_projector_shapes(const tsgb_projector* p, int64_t vol_shape[3],
                           int64_t sino_shape[3]);
 
+/* Plan statistics, written to out[0..n-1] (n <= 8):
+ *   [0] padded volume copies the forward projector builds (axis permutations)
+ *   [1] angles backprojected by the separable (det_v along z) gather kernel
+ *   [2] angles backprojected by the general gather kernel
+ *   [3] kernel launches per tsgb_direct_fp call
+ *   [4] kernel launches per matched tsgb_direct_bp call
+ *   [5] kernel launches per bilinear tsgb_direct_bp call
+ *   [6] forward workspace bytes, [7] matched backprojection workspace bytes
+ * No counterpart in ASTRA's projector; used for measurement and tests. */
+int tsgb_projector_stats(const tsgb_projector* p, int64_t* out, int32_t n);
+
 /* Message for the calling thread's most recent error ("" if none). */
 const char* tsgb_last_error(void);
 

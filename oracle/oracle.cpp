@@ -81,10 +81,13 @@ int dominant_axis(const Geo& g, const double* row) {
 }
 
 // Visit every (voxel, weight) pair of one ray: origin o and direction r in
-// voxel index coordinates, dominant axis d. f(flat_index, weight).
+// voxel index coordinates, dominant axis d. Only voxels with z in
+// [z_lo, z_hi) are visited (the full range by default). f(flat_index, weight).
 template <typename F>
-void walk_ray(const Geo& g, int d, const double* o, const double* r, F&& f) {
-  const int a = d == 0 ? 1 : 0;
+void walk_ray(const Geo& g, int d, const double* o, const double* r, F&& f, int64_t z_lo = 0,
+              int64_t z_hi = -1) {
+  if (z_hi < 0) z_hi = g.n[0];
+  const int a = d == 0 ? 1 : 0;  // for d != 0 the first in-plane axis is z
   const int b = d == 2 ? 1 : 2;
   if (r[d] == 0.0) return;
   const double sa = r[a] / r[d], sb = r[b] / r[d];
@@ -96,7 +99,23 @@ void walk_ray(const Geo& g, int d, const double* o, const double* r, F&& f) {
   }
   const double step = std::sqrt(step2);
   const int64_t stride[3] = {g.n[1] * g.n[2], g.n[2], 1};
-  for (int64_t k = 0; k < g.n[d]; ++k) {
+  // planes whose z taps can reach [z_lo, z_hi)
+  int64_t k0 = 0, k1 = g.n[d] - 1;
+  if (d == 0) {
+    k0 = std::max<int64_t>(k0, z_lo);
+    k1 = std::min<int64_t>(k1, z_hi - 1);
+  } else if (z_lo > 0 || z_hi < g.n[0]) {
+    // z(k) = o[0] + (k - o[d]) * sa must lie in (z_lo - 1, z_hi)
+    if (sa == 0.0) {
+      if (!(o[0] > z_lo - 1 && o[0] < z_hi)) return;
+    } else {
+      double t1 = o[d] + (z_lo - 1 - o[0]) / sa, t2 = o[d] + (z_hi - o[0]) / sa;
+      if (t1 > t2) std::swap(t1, t2);
+      k0 = std::max<int64_t>(k0, int64_t(std::floor(std::max(t1, -1.0))));
+      k1 = std::min<int64_t>(k1, int64_t(std::ceil(std::min(t2, double(g.n[d])))));
+    }
+  }
+  for (int64_t k = k0; k <= k1; ++k) {
     const double t = (double(k) - o[d]) / r[d];
     const double qa = o[a] + t * r[a], qb = o[b] + t * r[b];
     const double fa = std::floor(qa), fb = std::floor(qb);
@@ -105,6 +124,7 @@ void walk_ray(const Geo& g, int d, const double* o, const double* r, F&& f) {
     for (int da = 0; da < 2; ++da) {
       const int64_t i = ia + da;
       if (i < 0 || i >= g.n[a]) continue;
+      if (d != 0 && (i < z_lo || i >= z_hi)) continue;  // a == z here
       const double wa = da ? wa1 : 1.0 - wa1;
       for (int db = 0; db < 2; ++db) {
         const int64_t j = ib + db;
@@ -160,55 +180,59 @@ int check(const tsgb_volume_desc* v, const tsgb_projection_desc* p) {
 extern "C" {
 
 // sino[rows][angles][cols] = A vol, with det_ss x det_ss rays per pixel averaged.
+// Parallel over (angle, detector row).
 int oracle_fp(const tsgb_volume_desc* v, const tsgb_projection_desc* p, int det_ss,
               const double* vol, double* sino, int nthreads) {
   if (check(v, p) || det_ss < 1) return -1;
   const Geo g = make_geo(v, p);
   const double inv = 1.0 / (double(det_ss) * det_ss);
-  parallel_for(g.nangles, nthreads, [&](int64_t t, int) {
+  parallel_for(g.nangles * g.rows, nthreads, [&](int64_t item, int) {
+    const int64_t t = item / g.rows;
+    const int iv = int(item % g.rows);
     const int d = dominant_axis(g, g.vec + 12 * t);
-    for (int iv = 0; iv < g.rows; ++iv)
-      for (int iu = 0; iu < g.cols; ++iu) {
-        double acc = 0.0;
-        for (int s1 = 0; s1 < det_ss; ++s1)
-          for (int s2 = 0; s2 < det_ss; ++s2) {
-            double o[3], r[3];
-            make_ray(g, t, iv, iu, (s1 + 0.5) / det_ss - 0.5, (s2 + 0.5) / det_ss - 0.5, o, r);
-            walk_ray(g, d, o, r, [&](int64_t idx, double w) { acc += w * vol[idx]; });
-          }
-        sino[(int64_t(iv) * g.nangles + t) * g.cols + iu] = acc * inv;
-      }
+    for (int iu = 0; iu < g.cols; ++iu) {
+      double acc = 0.0;
+      for (int s1 = 0; s1 < det_ss; ++s1)
+        for (int s2 = 0; s2 < det_ss; ++s2) {
+          double o[3], r[3];
+          make_ray(g, t, iv, iu, (s1 + 0.5) / det_ss - 0.5, (s2 + 0.5) / det_ss - 0.5, o, r);
+          walk_ray(g, d, o, r, [&](int64_t idx, double w) { acc += w * vol[idx]; });
+        }
+      sino[(int64_t(iv) * g.nangles + t) * g.cols + iu] = acc * inv;
+    }
   });
   return 0;
 }
 
-// vol = A^T sino: the exact transpose of oracle_fp.
+// vol = A^T sino: the exact transpose of oracle_fp, by scattering every ray's
+// weights. Parallel over disjoint z slabs: each thread walks every ray but
+// only visits the voxels of its own slab, so no two threads write the same
+// voxel and the summation order is fixed (deterministic).
 int oracle_bp_matched(const tsgb_volume_desc* v, const tsgb_projection_desc* p, int det_ss,
                       const double* sino, double* vol, int nthreads) {
   if (check(v, p) || det_ss < 1) return -1;
   const Geo g = make_geo(v, p);
   const int64_t nvox = g.n[0] * g.n[1] * g.n[2];
-  nthreads = std::max(1, nthreads);
-  std::vector<std::vector<double>> part(nthreads, std::vector<double>(nvox, 0.0));
-  const double inv = 1.0 / (double(det_ss) * det_ss);
-  parallel_for(g.nangles, nthreads, [&](int64_t t, int tid) {
-    std::vector<double>& out = part[tid];
-    const int d = dominant_axis(g, g.vec + 12 * t);
-    for (int iv = 0; iv < g.rows; ++iv)
-      for (int iu = 0; iu < g.cols; ++iu) {
-        const double y = sino[(int64_t(iv) * g.nangles + t) * g.cols + iu] * inv;
-        if (y == 0.0) continue;
-        for (int s1 = 0; s1 < det_ss; ++s1)
-          for (int s2 = 0; s2 < det_ss; ++s2) {
-            double o[3], r[3];
-            make_ray(g, t, iv, iu, (s1 + 0.5) / det_ss - 0.5, (s2 + 0.5) / det_ss - 0.5, o, r);
-            walk_ray(g, d, o, r, [&](int64_t idx, double w) { out[idx] += w * y; });
-          }
-      }
-  });
   std::fill(vol, vol + nvox, 0.0);
-  for (int t = 0; t < nthreads; ++t)
-    for (int64_t i = 0; i < nvox; ++i) vol[i] += part[t][i];
+  const double inv = 1.0 / (double(det_ss) * det_ss);
+  const int64_t nslab = std::min<int64_t>(g.n[0], std::max(1, nthreads) * 2);
+  parallel_for(nslab, nthreads, [&](int64_t slab, int) {
+    const int64_t z_lo = g.n[0] * slab / nslab, z_hi = g.n[0] * (slab + 1) / nslab;
+    for (int64_t t = 0; t < g.nangles; ++t) {
+      const int d = dominant_axis(g, g.vec + 12 * t);
+      for (int iv = 0; iv < g.rows; ++iv)
+        for (int iu = 0; iu < g.cols; ++iu) {
+          const double y = sino[(int64_t(iv) * g.nangles + t) * g.cols + iu] * inv;
+          if (y == 0.0) continue;
+          for (int s1 = 0; s1 < det_ss; ++s1)
+            for (int s2 = 0; s2 < det_ss; ++s2) {
+              double o[3], r[3];
+              make_ray(g, t, iv, iu, (s1 + 0.5) / det_ss - 0.5, (s2 + 0.5) / det_ss - 0.5, o, r);
+              walk_ray(g, d, o, r, [&](int64_t idx, double w) { vol[idx] += w * y; }, z_lo, z_hi);
+            }
+        }
+    }
+  });
   return 0;
 }
 

@@ -60,6 +60,9 @@ SIGNATURES = {
     "tsgb_projector_shapes": (
         ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_int64), ctypes.POINTER(ctypes.c_int64)]
     ),
+    "tsgb_projector_stats": (
+        ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_int64), ctypes.c_int32]
+    ),
     "tsgb_last_error": (ctypes.c_char_p, []),
 }
 

@@ -87,6 +87,17 @@ class Projector:
             return int(lib.tsgb_fp_workspace_bytes(h))
         return int(lib.tsgb_bp_workspace_bytes(h, BP_KINDS[bp_kind]))
 
+    def stats(self, device_index):
+        """Plan statistics of the native projector (see tsgb_projector_stats)."""
+        lib = _native.load()
+        out = (ctypes.c_int64 * 8)()
+        _native.check(lib.tsgb_projector_stats(self.handle(device_index), out, 8),
+                      "tsgb_projector_stats")
+        keys = ["layouts", "separable_bp_angles", "general_bp_angles", "fp_launches",
+                "bp_matched_launches", "bp_bilinear_launches", "fp_workspace_bytes",
+                "bp_workspace_bytes"]
+        return dict(zip(keys, [int(v) for v in out]))
+
     def __del__(self):
         handles, self._handles = getattr(self, "_handles", {}), {}
         if handles and _native._lib is not None:
@@ -169,11 +180,9 @@ def direct_project(projector, vol_link, proj_link, forward=None, additive=False,
                                     BP_KINDS[bp_kind], ws.data_ptr(), nbytes, stream)
         _native.check(rc, "tsgb_direct_fp" if forward else "tsgb_direct_bp")
     if copy_back:
-        host = d_dst.cpu()
-        if isinstance(dst, np.ndarray):
-            np.copyto(dst, host.numpy())
-        else:
-            dst.copy_(host)
+        # Straight device -> host copy into the caller's buffer (a DMA when it is pinned).
+        target = torch.from_numpy(dst) if isinstance(dst, np.ndarray) else dst
+        target.copy_(d_dst)
 
 
 def direct_fp(projector, vol_data, proj_data, additive=False):
