@@ -62,8 +62,8 @@ def config(extra=None):
         "angles": ANGLES,
         "detector": list(DET),
         "phantom": "20 seeded random ellipsoids, densities U[0.1,1] (seed 2)",
-        "l2": f"inputs larger than L2 (volume {4 * N ** 3 / 1e9:.2f} GB, sinogram "
-        f"{4 * DET[0] * DET[1] * ANGLES / 1e9:.2f} GB; L2 129 MB)",
+        "l2": f"no L2 flush; every step streams a {4 * N ** 3 / 1e9:.2f} GB volume and a "
+        f"{4 * DET[0] * DET[1] * ANGLES / 1e9:.2f} GB sinogram (L2 is 129 MB)",
     }
     if extra:
         c.update(extra)
@@ -156,6 +156,7 @@ def cpu_baseline_sample(threads=None, angles=None):
     from oracle import oracle as orc
 
     threads = threads or (os.cpu_count() or 1)
+    vg, pg = workload_geometry(ts)
     # one angle per thread, at least 8: about 10-20 s of CPU work
     n_angles = angles or max(8, min(threads, 32))
     sub = pg[:: ANGLES // n_angles][:n_angles]
