@@ -31,7 +31,8 @@ namespace {
 constexpr float kMaxSlope = 64.0f;  // must match fp.cu
 constexpr int kBpX = 32;            // threads along x (one warp)
 constexpr int kBpY = 4;             // warps along y
-constexpr int kRunZ = 8;            // voxels along z per thread
+constexpr int kRunZ = 16;           // voxels along z per thread (matched)
+constexpr int kRunZBil = 8;         // voxels along z per thread (bilinear)
 
 __global__ void __launch_bounds__(256)
     bp_weight_kernel(const AngleParams* __restrict__ params,
@@ -51,7 +52,17 @@ __global__ void __launch_bounds__(256)
   out[idx] = w * __ldg(sino + idx);
 }
 
-// One thread per (x, y) voxel column and run of kRunZ voxels along z.
+// Detector value y'[iv][theta][iu] through a column pointer, zero outside
+// the detector rows. Offsets are 32-bit when the sinogram has < 2^31 floats.
+template <bool kWide>
+__device__ __forceinline__ float column_value(const float* __restrict__ col, int iv, int rows,
+                                              unsigned row_stride32, size_t row_stride) {
+  if (iv < 0 || iv >= rows) return 0.0f;
+  return kWide ? __ldg(col + (size_t)iv * row_stride) : __ldg(col + (unsigned)iv * row_stride32);
+}
+
+// One thread per (x, y) voxel column and run of kRun voxels along z.
+template <int kRun, bool kWide>
 __global__ void __launch_bounds__(kBpX* kBpY)
     bp_separable_kernel(const AngleParams* __restrict__ params,
                         const ColumnEntry* __restrict__ columns, const int* __restrict__ angles,
@@ -59,14 +70,16 @@ __global__ void __launch_bounds__(kBpX* kBpY)
                         DeviceGeometry g, int additive) {
   const int x = blockIdx.x * kBpX + threadIdx.x;
   const int y = blockIdx.y * kBpY + threadIdx.y;
-  const int z0 = blockIdx.z * kRunZ;
+  const int z0 = blockIdx.z * kRun;
   if (x >= g.nx || y >= g.ny) return;
   const float xt = float(x - g.ox), yt = float(y - g.oy);
   const float zt0 = float(z0 - g.oz);
   const size_t row_stride = (size_t)g.nangles * g.cols;
-  float acc[kRunZ];
+  const unsigned row_stride32 = (unsigned)row_stride;
+  const float4* __restrict__ col4 = reinterpret_cast<const float4*>(columns);
+  float acc[kRun];
 #pragma unroll
-  for (int j = 0; j < kRunZ; ++j) acc[j] = 0.0f;
+  for (int j = 0; j < kRun; ++j) acc[j] = 0.0f;
 
   for (int n = 0; n < n_angles; ++n) {
     const int theta = __ldg(angles + n);
@@ -74,44 +87,62 @@ __global__ void __launch_bounds__(kBpX* kBpY)
     // b = z here, so (d, a) is (x, y) or (y, x).
     const float kt = ap.d == 2 ? xt : yt;
     const float it = ap.d == 2 ? yt : xt;
-    // Columns whose rays hit plane kt within one voxel of it: solve
-    // (A0 + A1 u) / (e0 + e1 u) = it -+ 1 for u.
+    // Columns whose rays pass plane kt within one voxel of it: solve
+    // (A0 + A1 u) / (e0 + e1 u) = it -+ 1 for u. Only the range needs this;
+    // the weights below are exact, so fast division is enough.
     const float A0 = fmaf(kt, ap.ma[0], ap.ca[0]);
     const float A1 = fmaf(kt, ap.ma[1], ap.ca[1]);
     const float tl = it - 1.0f, th = it + 1.0f;
-    const float u1 = (tl * ap.e[0] - A0) / (A1 - tl * ap.e[1]);
-    const float u2 = (th * ap.e[0] - A0) / (A1 - th * ap.e[1]);
-    if (isnan(u1) || isnan(u2)) continue;
-    const float ulo = clamp_coord(fminf(u1, u2)), uhi = clamp_coord(fmaxf(u1, u2));
-    const int iu_lo = max(0, (int)floorf(ulo) + 1 + g.ou);
-    const int iu_hi = min(g.cols - 1, (int)ceilf(uhi) - 1 + g.ou);
+    const float u1 = __fdividef(fmaf(tl, ap.e[0], -A0), fmaf(-tl, ap.e[1], A1));
+    const float u2 = __fdividef(fmaf(th, ap.e[0], -A0), fmaf(-th, ap.e[1], A1));
+    const int iu_lo = max(0, (int)floorf(clamp_coord(fminf(u1, u2))) + 1 + g.ou);
+    const int iu_hi = min(g.cols - 1, (int)ceilf(clamp_coord(fmaxf(u1, u2))) - 1 + g.ou);
+    const float* __restrict__ sino_theta = sinow + (size_t)theta * g.cols;
     for (int iu = iu_lo; iu <= iu_hi; ++iu) {
-      const ColumnEntry c = columns[(size_t)theta * g.cols + iu];
-      const float h = 1.0f - fabsf(fmaf(kt, c.ma, c.Xa) - it);
+      const size_t ci = ((size_t)theta * g.cols + iu) * 2;
+      const float4 c0 = __ldg(col4 + ci);  // Xa, ma, P, Q
+      const float4 c1 = __ldg(col4 + ci + 1);  // R, S, -, -
+      const float h = 1.0f - fabsf(fmaf(kt, c0.y, c0.x) - it);
       if (h <= 0.0f) continue;
-      // q_b(vt) = B + vt * Sl on this plane
-      const float B = fmaf(kt, c.Q, c.P);
-      const float Sl = fmaf(kt, c.S, c.R);
-      const float inv = 1.0f / Sl;
-      const float* col = sinow + (size_t)theta * g.cols + iu;
+      // On plane kt, q_b(vt) = B + vt * Sl.
+      const float B = fmaf(kt, c0.w, c0.z);
+      const float Sl = fmaf(kt, c1.y, c1.x);
+      const float inv = __fdividef(1.0f, Sl);
+      const float* __restrict__ col = sino_theta + iu;
+      if (fabsf(Sl) >= 1.0f) {
+        // Tent half-width 1/|Sl| <= 1 row: only rows floor(v*) and floor(v*)+1.
+        const float vs0 = (zt0 - B) * inv;
 #pragma unroll
-      for (int j = 0; j < kRunZ; ++j) {
-        const float Bj = B - (zt0 + float(j));
-        const float v1 = (-1.0f - Bj) * inv, v2 = (1.0f - Bj) * inv;
-        const float vlo = clamp_coord(fminf(v1, v2)), vhi = clamp_coord(fmaxf(v1, v2));
-        const int iv_lo = max(0, (int)floorf(vlo) + 1 + g.ov);
-        const int iv_hi = min(g.rows - 1, (int)ceilf(vhi) - 1 + g.ov);
-        float s = 0.0f;
-        for (int iv = iv_lo; iv <= iv_hi; ++iv) {
-          const float w = tent(fmaf(float(iv - g.ov), Sl, Bj));
-          s = fmaf(w, __ldg(col + (size_t)iv * row_stride), s);
+        for (int j = 0; j < kRun; ++j) {
+          const float vs = fmaf(float(j), inv, vs0);
+          const float v0 = floorf(clamp_coord(vs));
+          const float Bj = B - (zt0 + float(j));
+          const float w0 = tent(fmaf(v0, Sl, Bj));
+          const float w1 = tent(fmaf(v0 + 1.0f, Sl, Bj));
+          const int iv0 = (int)v0 + g.ov;
+          const float y0 = column_value<kWide>(col, iv0, g.rows, row_stride32, row_stride);
+          const float y1 = column_value<kWide>(col, iv0 + 1, g.rows, row_stride32, row_stride);
+          acc[j] = fmaf(h, fmaf(w0, y0, w1 * y1), acc[j]);
         }
-        acc[j] = fmaf(h, s, acc[j]);
+      } else {
+#pragma unroll
+        for (int j = 0; j < kRun; ++j) {
+          const float Bj = B - (zt0 + float(j));
+          const float v1 = (-1.0f - Bj) * inv, v2 = (1.0f - Bj) * inv;
+          const int iv_lo = max(0, (int)floorf(clamp_coord(fminf(v1, v2))) + g.ov);
+          const int iv_hi = min(g.rows - 1, (int)ceilf(clamp_coord(fmaxf(v1, v2))) + g.ov);
+          float s = 0.0f;
+          for (int iv = iv_lo; iv <= iv_hi; ++iv) {
+            const float w = tent(fmaf(float(iv - g.ov), Sl, Bj));
+            s = fmaf(w, column_value<kWide>(col, iv, g.rows, row_stride32, row_stride), s);
+          }
+          acc[j] = fmaf(h, s, acc[j]);
+        }
       }
     }
   }
 #pragma unroll
-  for (int j = 0; j < kRunZ; ++j) {
+  for (int j = 0; j < kRun; ++j) {
     const int z = z0 + j;
     if (z < g.nz) {
       float* out = vol + ((size_t)z * g.ny + y) * g.nx + x;
@@ -221,15 +252,15 @@ __global__ void __launch_bounds__(kBpX* kBpY)
                        float* __restrict__ vol, DeviceGeometry g, int additive) {
   const int x = blockIdx.x * kBpX + threadIdx.x;
   const int y = blockIdx.y * kBpY + threadIdx.y;
-  const int z0 = blockIdx.z * kRunZ;
+  const int z0 = blockIdx.z * kRunZBil;
   if (x >= g.nx || y >= g.ny) return;
   const bool cone = g.kind == TSGB_CONE;
   const size_t row_stride = (size_t)g.nangles * g.cols;
   const int ss = g.vox_ss;
   const float inv_ss = 1.0f / float(ss);
-  float acc[kRunZ];
+  float acc[kRunZBil];
 #pragma unroll
-  for (int j = 0; j < kRunZ; ++j) acc[j] = 0.0f;
+  for (int j = 0; j < kRunZBil; ++j) acc[j] = 0.0f;
   for (int theta = 0; theta < g.nangles; ++theta) {
     const AngleParams& ap = params[theta];
     const float* base = sino + (size_t)theta * g.cols;
@@ -240,7 +271,7 @@ __global__ void __launch_bounds__(kBpX* kBpY)
           const float oz = (sz + 0.5f) * inv_ss - 0.5f;
           const float xt = float(x - g.ox) + ox, yt = float(y - g.oy) + oy;
 #pragma unroll
-          for (int j = 0; j < kRunZ; ++j) {
+          for (int j = 0; j < kRunZBil; ++j) {
             const float zt = float(z0 + j - g.oz) + oz;
             const float nu = fmaf(ap.pu[0], zt, fmaf(ap.pu[1], yt, fmaf(ap.pu[2], xt, ap.pu[3])));
             const float nv = fmaf(ap.pv[0], zt, fmaf(ap.pv[1], yt, fmaf(ap.pv[2], xt, ap.pv[3])));
@@ -261,7 +292,7 @@ __global__ void __launch_bounds__(kBpX* kBpY)
   }
   const float norm = inv_ss * inv_ss * inv_ss;
 #pragma unroll
-  for (int j = 0; j < kRunZ; ++j) {
+  for (int j = 0; j < kRunZBil; ++j) {
     const int z = z0 + j;
     if (z < g.nz) {
       float* out = vol + ((size_t)z * g.ny + y) * g.nx + x;
@@ -294,9 +325,15 @@ int launch_bp_matched(const tsgb_projector* p, float* vol, const float* sino, bo
   if (p->n_separable_bp > 0) {
     const dim3 block(kBpX, kBpY);
     const dim3 grid((g.nx + kBpX - 1) / kBpX, (g.ny + kBpY - 1) / kBpY, (g.nz + kRunZ - 1) / kRunZ);
-    bp_separable_kernel<<<grid, block, 0, stream>>>(p->d_params, p->d_columns, p->d_sep_angles,
-                                                    p->n_separable_bp, workspace, vol, g,
-                                                    additive ? 1 : 0);
+    const bool wide = (size_t)g.rows * g.nangles * g.cols >= (size_t(1) << 31);
+    if (wide)
+      bp_separable_kernel<kRunZ, true><<<grid, block, 0, stream>>>(
+          p->d_params, p->d_columns, p->d_sep_angles, p->n_separable_bp, workspace, vol, g,
+          additive ? 1 : 0);
+    else
+      bp_separable_kernel<kRunZ, false><<<grid, block, 0, stream>>>(
+          p->d_params, p->d_columns, p->d_sep_angles, p->n_separable_bp, workspace, vol, g,
+          additive ? 1 : 0);
     written = true;
   }
   if (p->n_general_bp > 0 || !written) {
@@ -314,7 +351,7 @@ int launch_bp_bilinear(const tsgb_projector* p, float* vol, const float* sino, b
   cudaStream_t stream = static_cast<cudaStream_t>(stream_);
   const DeviceGeometry& g = p->g;
   const dim3 block(kBpX, kBpY);
-  const dim3 grid((g.nx + kBpX - 1) / kBpX, (g.ny + kBpY - 1) / kBpY, (g.nz + kRunZ - 1) / kRunZ);
+  const dim3 grid((g.nx + kBpX - 1) / kBpX, (g.ny + kBpY - 1) / kBpY, (g.nz + kRunZBil - 1) / kRunZBil);
   bp_bilinear_kernel<<<grid, block, 0, stream>>>(p->d_params, sino, vol, g, additive ? 1 : 0);
   return int(cudaGetLastError());
 }

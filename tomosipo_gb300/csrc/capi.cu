@@ -78,9 +78,10 @@ int tsgb_projector_create(const tsgb_volume_desc* vol, const tsgb_projection_des
       delete p;
       return fail(TSGB_ERR_INVALID, "volume too large for 32-bit indexing of one padded copy");
     }
-  if (p->g.nz > 65535 || p->g.rows > 4 * 65535) {
+  if (p->g.nz > 65535 || p->g.rows > 4 * 65535 || p->g.cols > 8 * 65535) {
     delete p;
-    return fail(TSGB_ERR_INVALID, "volume z extent must be <= 65535 and detector rows <= 262140");
+    return fail(TSGB_ERR_INVALID,
+                "volume z extent must be <= 65535, detector rows <= 262140 and columns <= 524280");
   }
   cudaError_t e = cudaGetDevice(&p->device);
   if (e == cudaSuccess) e = upload(&p->d_params, p->host_params);

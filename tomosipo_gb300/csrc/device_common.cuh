@@ -7,15 +7,13 @@
 
 namespace tsgb {
 
-// Per-layout addressing of a padded forward-projection volume copy.
-// Element (k along d, i along a, j along b), all unpadded indices, lives at
-//   base + (j + kPad) * stride_b + k * stride_d + (i + kPad)
-// with stride_d = n_a + 2 kPad and stride_b = n_d * stride_d (a fastest).
+// Per-layout description of a padded forward-projection volume copy, laid
+// out [d][a][b] (b fastest) with kPad zero voxels on both sides of a and b.
 struct LayoutDev {
   long long offset;
   int n_d, n_a, n_b;
   int o_d, o_a, o_b;
-  int stride_d, stride_b;
+  int stride_d, stride_a;
 };
 
 struct LayoutTable {
@@ -37,8 +35,8 @@ __host__ inline LayoutTable make_layout_table(const tsgb_projector* p) {
     D.o_d = anchors[L.d];
     D.o_a = anchors[L.a];
     D.o_b = anchors[L.b];
-    D.stride_d = int(L.n_a + 2 * kPad);
-    D.stride_b = int(L.n_d * (L.n_a + 2 * kPad));
+    D.stride_a = int(L.n_b + 2 * kPad);
+    D.stride_d = int((L.n_a + 2 * kPad) * (L.n_b + 2 * kPad));
   }
   return t;
 }

@@ -279,8 +279,8 @@ std::string build_plan(const tsgb_volume_desc* vol, const tsgb_projection_desc* 
     ap.o_d = anchor[L.d];
     ap.o_a = anchor[L.a];
     ap.o_b = anchor[L.b];
-    ap.stride_d = int(L.n_a + 2 * kPad);
-    ap.stride_b = int(L.n_d * (L.n_a + 2 * kPad));
+    ap.stride_a = int(L.n_b + 2 * kPad);
+    ap.stride_d = int((L.n_a + 2 * kPad) * (L.n_b + 2 * kPad));
     ap.vs_d = float(vs[L.d]);
     ap.vs_a = float(vs[L.a]);
     ap.vs_b = float(vs[L.b]);

@@ -49,13 +49,13 @@ struct alignas(16) AngleParams {
   // cone: bil_scale * |P - src|_world / (pw . [P,1])^3.
   float bil_scale;
   float src[3];      // source in anchored voxel coordinates (cone)
-  // Addressing of this angle's padded forward-projection copy: element
-  // (k along d, i along a, j along b; unpadded indices) is at
-  //   ws_offset + (j + kPad) * stride_b + k * stride_d + (i + kPad).
+  // Addressing of this angle's padded forward-projection copy, laid out
+  // [d][a][b] with b fastest: element (k along d, i along a, j along b;
+  // unpadded indices) is at ws_offset + k * stride_d + (i + kPad) * stride_a + (j + kPad).
   long long ws_offset;
   int n_d, n_a, n_b;
   int o_d, o_a, o_b;
-  int stride_d, stride_b;
+  int stride_d, stride_a;
   float vs_d, vs_a, vs_b;  // voxel size along d, a, b (world units)
   float pad2;
 };
@@ -72,7 +72,7 @@ struct Layout {
   int d, a, b;
   int64_t n_d, n_a, n_b;   // unpadded extents
   int64_t offset_floats;   // offset of this copy in the forward workspace
-  int64_t floats() const { return (n_b + 2 * kPad) * n_d * (n_a + 2 * kPad); }
+  int64_t floats() const { return n_d * (n_a + 2 * kPad) * (n_b + 2 * kPad); }
 };
 
 struct DeviceGeometry {
