@@ -93,6 +93,23 @@ int tsgb_direct_bp(tsgb_projector* p, float* vol, const float* sino,
                    int32_t additive, int32_t bp_kind, void* workspace,
                    int64_t workspace_bytes, void* stream);
 
+/* Forward projection sino = A(vol) (sino += ... when ``additive``) that allocates
+ * no device memory, for callers that cannot call cudaMalloc: code running inside
+ * another framework's allocator (a custom-call hook) or a real-time loop with a
+ * fixed memory budget. It takes the geometry directly (no projector) plus the
+ * caller's input and output, and keeps its scratch -- the padded volume copies
+ * and the per-angle parameters -- in fixed static device arrays: at most
+ * 16,777,216 floats (64 MiB) of copies (sum of n_d * (n_a + 4) * (n_b + 4) over
+ * the axis permutations used; two copies of a 160^3 volume fit) and at most
+ * 4096 angles; larger requests fail with TSGB_ERR_INVALID. The first call on
+ * each device resolves the arrays' addresses (make it before any stream
+ * capture); the arrays then stay allocated on that device until exit. Calls
+ * share the arrays, so calls that overlap on the GPU race: keep them on one
+ * stream. No counterpart in the reference (tomosipo / ASTRA). */
+int tsgb_direct_fp_noalloc(const tsgb_volume_desc* vol, const tsgb_projection_desc* proj,
+                           const float* vol_in, float* sino_out, int32_t additive,
+                           void* stream);
+
 /* Shapes the projector expects: vol (z, y, x) and sino (rows, angles, cols). */
 int tsgb_projector_shapes(const tsgb_projector* p, int64_t vol_shape[3],
                           int64_t sino_shape[3]);

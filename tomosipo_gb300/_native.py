@@ -63,6 +63,11 @@ SIGNATURES = {
     "tsgb_projector_stats": (
         ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_int64), ctypes.c_int32]
     ),
+    "tsgb_direct_fp_noalloc": (
+        ctypes.c_int,
+        [ctypes.POINTER(VolumeDesc), ctypes.POINTER(ProjectionDesc), ctypes.c_void_p,
+         ctypes.c_void_p, ctypes.c_int32, ctypes.c_void_p],
+    ),
     "tsgb_last_error": (ctypes.c_char_p, []),
 }
 

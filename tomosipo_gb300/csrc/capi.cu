@@ -55,6 +55,10 @@ int check_device(const tsgb_projector* p) {
 
 }  // namespace
 
+namespace tsgb {
+void set_last_error(const std::string& msg) { g_last_error = msg; }
+}  // namespace tsgb
+
 extern "C" {
 
 int tsgb_projector_create(const tsgb_volume_desc* vol, const tsgb_projection_desc* proj,

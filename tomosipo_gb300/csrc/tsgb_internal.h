@@ -111,6 +111,9 @@ std::string build_plan(const tsgb_volume_desc* vol, const tsgb_projection_desc* 
                        std::vector<ColumnEntry>* columns,
                        std::vector<int>* sep_angles, std::vector<int>* gen_angles);
 
+// Sets the calling thread's message returned by tsgb_last_error (capi.cu).
+void set_last_error(const std::string& msg);
+
 // Kernel launchers (fp.cu, bp.cu). All return cudaGetLastError() as int.
 int launch_fp(const tsgb_projector* p, const float* vol, float* sino, bool additive,
               float* workspace, void* stream);
