@@ -110,6 +110,36 @@ int tsgb_direct_fp_noalloc(const tsgb_volume_desc* vol, const tsgb_projection_de
                            const float* vol_in, float* sino_out, int32_t additive,
                            void* stream);
 
+/* One job of a batched SIRT solve: x += C * A^T(R * (y - A x)) per iteration.
+ * All buffers are device memory on the projector's device: vol, C (volume
+ * shaped), sino, R, residual (sinogram shaped), fp_workspace
+ * (tsgb_fp_workspace_bytes). The job's angles must all use the separable
+ * backprojector (det_v along z: circular and helical geometries). */
+typedef struct {
+  tsgb_projector* projector;
+  float* vol;
+  const float* sino;
+  const float* R;
+  const float* C;
+  float* residual;
+  float* fp_workspace;
+} tsgb_sirt_job;
+
+typedef struct tsgb_sirt_batch tsgb_sirt_batch;
+
+/* Build the device job tables of a batch (one small allocation). No
+ * counterpart in the reference, whose SIRT is a Python loop per job
+ * (README.md:150-163); results equal that loop's. */
+int tsgb_sirt_batch_create(const tsgb_sirt_job* jobs, int32_t n_jobs, tsgb_sirt_batch** out);
+
+/* Run ``iterations`` SIRT iterations of every job: three kernel launches per
+ * iteration over all jobs, on ``stream``. Allocates nothing; capturable in a
+ * CUDA graph. */
+int tsgb_sirt_batch_iterate(tsgb_sirt_batch* b, int32_t iterations, void* stream);
+
+/* Free a batch's tables (not the jobs' buffers). */
+int tsgb_sirt_batch_destroy(tsgb_sirt_batch* b);
+
 /* Shapes the projector expects: vol (z, y, x) and sino (rows, angles, cols). */
 int tsgb_projector_shapes(const tsgb_projector* p, int64_t vol_shape[3],
                           int64_t sino_shape[3]);

@@ -1,0 +1,92 @@
+"""SIRT: the reference recipe, the batched solver, and agreement between them."""
+import numpy as np
+import pytest
+
+import tomosipo_gb300 as ts
+from oracle import oracle as orc
+from tomosipo_gb300.sirt import BatchedSirt, preconditioners, sirt
+from tests.helpers import ellipsoid_phantom, rel_l2
+
+torch = pytest.importorskip("torch")
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def dev(native_lib):
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    return torch.device("cuda", 0)
+
+
+def _job(dev, n, cone, angles, seed):
+    vg = ts.volume(shape=n, size=1)
+    pg = (ts.cone(angles=angles, shape=(n, 3 * n // 2), size=np.sqrt(2), cone_angle=0.5) if cone
+          else ts.parallel(angles=angles, shape=(n, 3 * n // 2), size=(1, 1.5)))
+    A = ts.operator(vg, pg)
+    x = torch.from_numpy(ellipsoid_phantom(vg.shape, n=8, seed=seed)).to(dev)
+    y = A(x)
+    gen = torch.Generator(device="cpu").manual_seed(seed)
+    y = y + 0.01 * float(y.max()) * torch.randn(y.shape, generator=gen).to(dev)
+    return A, y, x
+
+
+def test_sirt_converges(dev):
+    A, y, x_true = _job(dev, 48, True, 72, seed=3)
+    errs = []
+    for n in (1, 5, 20):
+        errs.append(rel_l2(sirt(A, y, n).cpu().numpy(), x_true.cpu().numpy()))
+    assert errs[0] > errs[1] > errs[2]
+    res = [float(torch.linalg.norm(y - A(sirt(A, y, n)))) for n in (1, 5, 20)]
+    assert res[0] > res[1] > res[2]
+
+
+def test_sirt_matches_fp64_oracle(dev):
+    """10 iterations on the GPU (fp32) vs the same recipe with FP64 oracle operators."""
+    vg = ts.volume(shape=24, size=1)
+    pg = ts.cone(angles=30, shape=(24, 36), size=np.sqrt(2), cone_angle=0.5)
+    A = ts.operator(vg, pg)
+    x_true = ellipsoid_phantom(vg.shape, n=5, seed=9).astype(np.float64)
+    y = orc.fp(vg, pg, x_true)
+    x_gpu = sirt(A, torch.from_numpy(y.astype(np.float32)).to(dev), 10).cpu().numpy()
+    with np.errstate(divide="ignore"):
+        R = np.minimum(1 / orc.fp(vg, pg, np.ones(vg.shape)), 1e8)
+        C = np.minimum(1 / orc.bp_matched(vg, pg, np.ones(y.shape)), 1e8)
+    x = np.zeros(vg.shape)
+    for _ in range(10):
+        x += C * orc.bp_matched(vg, pg, R * (y - orc.fp(vg, pg, x)))
+    assert rel_l2(x_gpu, x) <= 1e-5
+
+
+def test_batched_equals_plain_and_alone_equals_mix(dev):
+    jobs = [_job(dev, 32, False, 40, 1), _job(dev, 48, True, 60, 2), _job(dev, 40, True, 50, 3),
+            _job(dev, 64, False, 90, 4)]
+    n_it = 6
+    plain = [sirt(A, y, n_it) for A, y, _ in jobs]
+    mix = BatchedSirt([(A, y) for A, y, _ in jobs])
+    mix.run(n_it, graph=False)
+    for a, b in zip(mix.x, plain):
+        assert torch.equal(a, b)
+    alone = BatchedSirt([(jobs[1][0], jobs[1][1])])
+    alone.run(n_it, graph=False)
+    assert torch.equal(alone.x[0], mix.x[1])
+
+
+def test_batched_graph_replay_equals_eager(dev):
+    jobs = [_job(dev, 32, True, 40, 5), _job(dev, 48, False, 70, 6)]
+    eager = BatchedSirt([(A, y) for A, y, _ in jobs])
+    eager.run(5, graph=False)
+    graphed = BatchedSirt([(A, y) for A, y, _ in jobs])
+    graphed.run(5, graph=True)
+    torch.cuda.synchronize()
+    for a, b in zip(eager.x, graphed.x):
+        assert torch.equal(a, b)
+
+
+def test_batched_rejects_tilted_detectors(dev):
+    vg = ts.volume(shape=16, size=1)
+    R = ts.rotate(pos=0, axis=(1.0, 0.5, 0.2), angles=0.5)
+    pg = R * ts.cone(angles=8, shape=(16, 24), size=1.5, src_orig_dist=3, src_det_dist=4).to_vec()
+    A = ts.operator(vg, pg)
+    y = torch.zeros(A.range_shape, device=dev)
+    with pytest.raises(RuntimeError, match="separable"):
+        BatchedSirt([(A, y)])

@@ -34,6 +34,18 @@ class ProjectionDesc(ctypes.Structure):
     ]
 
 
+class SirtJob(ctypes.Structure):
+    _fields_ = [
+        ("projector", ctypes.c_void_p),
+        ("vol", ctypes.c_void_p),
+        ("sino", ctypes.c_void_p),
+        ("R", ctypes.c_void_p),
+        ("C", ctypes.c_void_p),
+        ("residual", ctypes.c_void_p),
+        ("fp_workspace", ctypes.c_void_p),
+    ]
+
+
 _lib = None
 _lock = threading.Lock()
 
@@ -68,6 +80,11 @@ SIGNATURES = {
         [ctypes.POINTER(VolumeDesc), ctypes.POINTER(ProjectionDesc), ctypes.c_void_p,
          ctypes.c_void_p, ctypes.c_int32, ctypes.c_void_p],
     ),
+    "tsgb_sirt_batch_create": (
+        ctypes.c_int, [ctypes.POINTER(SirtJob), ctypes.c_int32, ctypes.POINTER(ctypes.c_void_p)]
+    ),
+    "tsgb_sirt_batch_iterate": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, ctypes.c_void_p]),
+    "tsgb_sirt_batch_destroy": (ctypes.c_int, [ctypes.c_void_p]),
     "tsgb_last_error": (ctypes.c_char_p, []),
 }
 

@@ -29,9 +29,9 @@ namespace tsgb {
 namespace {
 
 constexpr float kMaxSlope = 64.0f;  // must match fp.cu
-constexpr int kBpX = 32;            // threads along x (one warp)
-constexpr int kBpY = 4;             // warps along y
-constexpr int kRunZ = 16;           // voxels along z per thread (matched)
+constexpr int kBpX = kBpTileX;      // threads along x (one warp)
+constexpr int kBpY = kBpTileY;      // warps along y
+constexpr int kRunZ = kBpRunZ;      // voxels along z per thread (matched)
 constexpr int kRunZBil = 8;         // voxels along z per thread (bilinear)
 
 __global__ void __launch_bounds__(256)
@@ -61,23 +61,18 @@ __device__ __forceinline__ float column_value(const float* __restrict__ col, int
   return kWide ? __ldg(col + (size_t)iv * row_stride) : __ldg(col + (unsigned)iv * row_stride32);
 }
 
-// One thread per (x, y) voxel column and run of kRun voxels along z.
+// Matched backprojection of the angles in `angles` for the voxel column
+// (x, y) and the kRun voxels z0 .. z0 + kRun - 1, accumulated into acc.
 template <int kRun, bool kWide>
-__global__ void __launch_bounds__(kBpX* kBpY)
-    bp_separable_kernel(const AngleParams* __restrict__ params,
-                        const ColumnEntry* __restrict__ columns, const int* __restrict__ angles,
-                        int n_angles, const float* __restrict__ sinow, float* __restrict__ vol,
-                        DeviceGeometry g, int additive) {
-  const int x = blockIdx.x * kBpX + threadIdx.x;
-  const int y = blockIdx.y * kBpY + threadIdx.y;
-  const int z0 = blockIdx.z * kRun;
-  if (x >= g.nx || y >= g.ny) return;
+__device__ __forceinline__ void bp_separable_accumulate(
+    const AngleParams* __restrict__ params, const ColumnEntry* __restrict__ columns,
+    const int* __restrict__ angles, int n_angles, const float* __restrict__ sinow,
+    const DeviceGeometry& g, int x, int y, int z0, float (&acc)[kRun]) {
   const float xt = float(x - g.ox), yt = float(y - g.oy);
   const float zt0 = float(z0 - g.oz);
   const size_t row_stride = (size_t)g.nangles * g.cols;
   const unsigned row_stride32 = (unsigned)row_stride;
   const float4* __restrict__ col4 = reinterpret_cast<const float4*>(columns);
-  float acc[kRun];
 #pragma unroll
   for (int j = 0; j < kRun; ++j) acc[j] = 0.0f;
 
@@ -100,7 +95,7 @@ __global__ void __launch_bounds__(kBpX* kBpY)
     const float* __restrict__ sino_theta = sinow + (size_t)theta * g.cols;
     for (int iu = iu_lo; iu <= iu_hi; ++iu) {
       const size_t ci = ((size_t)theta * g.cols + iu) * 2;
-      const float4 c0 = __ldg(col4 + ci);  // Xa, ma, P, Q
+      const float4 c0 = __ldg(col4 + ci);      // Xa, ma, P, Q
       const float4 c1 = __ldg(col4 + ci + 1);  // R, S, -, -
       const float h = 1.0f - fabsf(fmaf(kt, c0.y, c0.x) - it);
       if (h <= 0.0f) continue;
@@ -141,6 +136,21 @@ __global__ void __launch_bounds__(kBpX* kBpY)
       }
     }
   }
+}
+
+// One thread per (x, y) voxel column and run of kRun voxels along z.
+template <int kRun, bool kWide>
+__global__ void __launch_bounds__(kBpX* kBpY)
+    bp_separable_kernel(const AngleParams* __restrict__ params,
+                        const ColumnEntry* __restrict__ columns, const int* __restrict__ angles,
+                        int n_angles, const float* __restrict__ sinow, float* __restrict__ vol,
+                        DeviceGeometry g, int additive) {
+  const int x = blockIdx.x * kBpX + threadIdx.x;
+  const int y = blockIdx.y * kBpY + threadIdx.y;
+  const int z0 = blockIdx.z * kRun;
+  if (x >= g.nx || y >= g.ny) return;
+  float acc[kRun];
+  bp_separable_accumulate<kRun, kWide>(params, columns, angles, n_angles, sinow, g, x, y, z0, acc);
 #pragma unroll
   for (int j = 0; j < kRun; ++j) {
     const int z = z0 + j;
@@ -150,6 +160,42 @@ __global__ void __launch_bounds__(kBpX* kBpY)
         *out += acc[j];
       else
         *out = acc[j];
+    }
+  }
+}
+
+// Batched SIRT backprojection over all jobs' voxel tiles; epilogue
+// x += C * A^T(res), rounded as the plain recipe's x += C * bp.
+template <int kRun>
+__global__ void __launch_bounds__(kBpX* kBpY)
+    bp_sirt_batch_kernel(const SirtJobDev* __restrict__ jobs, const long long* __restrict__ prefix,
+                         int n_jobs) {
+  const long long b = blockIdx.x;
+  const int jn = find_job(prefix, n_jobs, b);
+  const SirtJobDev& job = jobs[jn];
+  const DeviceGeometry& g = job.g;
+  long long local = b - prefix[jn];
+  const int xb = int(local % job.bp_xb);
+  local /= job.bp_xb;
+  const int yb = int(local % job.bp_yb);
+  const int zb = int(local / job.bp_yb);
+  const int x = xb * kBpX + threadIdx.x;
+  const int y = yb * kBpY + threadIdx.y;
+  const int z0 = zb * kRun;
+  if (x >= g.nx || y >= g.ny) return;
+  float acc[kRun];
+  if (job.wide)
+    bp_separable_accumulate<kRun, true>(job.params, job.columns, job.sep_angles, job.n_sep,
+                                        job.res, g, x, y, z0, acc);
+  else
+    bp_separable_accumulate<kRun, false>(job.params, job.columns, job.sep_angles, job.n_sep,
+                                         job.res, g, x, y, z0, acc);
+#pragma unroll
+  for (int j = 0; j < kRun; ++j) {
+    const int z = z0 + j;
+    if (z < g.nz) {
+      const size_t idx = ((size_t)z * g.ny + y) * g.nx + x;
+      job.vol[idx] = __fadd_rn(job.vol[idx], __fmul_rn(acc[j], __ldg(job.C + idx)));
     }
   }
 }
@@ -343,6 +389,14 @@ int launch_bp_matched(const tsgb_projector* p, float* vol, const float* sino, bo
                                                   p->n_general_bp, workspace, vol, g,
                                                   (additive || written) ? 1 : 0);
   }
+  return int(cudaGetLastError());
+}
+
+int launch_sirt_bp_batch(const SirtBatchDev& b, void* stream_) {
+  cudaStream_t stream = static_cast<cudaStream_t>(stream_);
+  if (b.bp_blocks > 0)
+    bp_sirt_batch_kernel<kRunZ><<<unsigned(b.bp_blocks), dim3(kBpX, kBpY), 0, stream>>>(
+        b.jobs, b.bp_prefix, b.n_jobs);
   return int(cudaGetLastError());
 }
 

@@ -22,8 +22,8 @@
 namespace tsgb {
 namespace {
 
-constexpr int kFpRows = 32;  // threads along detector rows (one warp)
-constexpr int kFpCols = 8;   // warps along detector columns
+constexpr int kFpRows = kFpTileRows;  // threads along detector rows (one warp)
+constexpr int kFpCols = kFpTileCols;  // warps along detector columns
 
 // Rays making more than ~89 degrees with the dominant axis are not sampled
 // (both here and, through the weighted sinogram, in the transpose).
@@ -76,20 +76,21 @@ __device__ __forceinline__ float bilinear_sample(const float* __restrict__ base,
   return fmaf(fa, right - left, left);
 }
 
-__global__ void __launch_bounds__(kFpRows* kFpCols)
-    fp_ray_kernel(const AngleParams* __restrict__ params, const ColumnEntry* __restrict__ columns,
-                  const float* __restrict__ ws, float* __restrict__ sino, DeviceGeometry g,
-                  int angle0, int additive) {
-  const int iv = blockIdx.x * kFpRows + threadIdx.x;
-  const int iu = blockIdx.y * kFpCols + threadIdx.y;
-  const int theta = angle0 + blockIdx.z;
-  if (iu >= g.cols || iv >= g.rows) return;
-  const AngleParams& ap = params[theta];
+// Ray sum of pixel (iv, iu) at angle theta, already scaled by the plane step.
+// W receives the plane step the transpose weights this ray with (0 for rays
+// that are not sampled), exactly as bp_weight_kernel computes it.
+__device__ __forceinline__ float fp_ray_total(const AngleParams& ap,
+                                              const ColumnEntry* __restrict__ columns,
+                                              const float* __restrict__ ws,
+                                              const DeviceGeometry& g, int iv, int iu, int theta,
+                                              float& W) {
   const float vt = float(iv - g.ov);
   const Ray r = ap.separable ? ray_column(columns[(size_t)theta * g.cols + iu], vt)
                              : ray_general(ap, float(iu - g.ou), vt);
   float total = 0.0f;
+  W = 0.0f;
   if (finite_ray(r) && fabsf(r.ma) <= kMaxSlope && fabsf(r.mb) <= kMaxSlope) {
+    W = ray_step(ap, r);
     const int o_d = ap.o_d, o_a = ap.o_a, o_b = ap.o_b;
     const int stride_d = ap.stride_d, stride_a = ap.stride_a;
     float klo = float(-o_d), khi = float(ap.n_d - 1 - o_d);
@@ -107,14 +108,70 @@ __global__ void __launch_bounds__(kFpRows* kFpCols)
         acc1 += bilinear_sample(base, r, k + 1, stride_d, stride_a);
       }
       if (k == k1) acc0 += bilinear_sample(base, r, k, stride_d, stride_a);
-      total = (acc0 + acc1) * ray_step(ap, r);
+      total = (acc0 + acc1) * W;
     }
   }
+  return total;
+}
+
+__global__ void __launch_bounds__(kFpRows* kFpCols)
+    fp_ray_kernel(const AngleParams* __restrict__ params, const ColumnEntry* __restrict__ columns,
+                  const float* __restrict__ ws, float* __restrict__ sino, DeviceGeometry g,
+                  int angle0, int additive) {
+  const int iv = blockIdx.x * kFpRows + threadIdx.x;
+  const int iu = blockIdx.y * kFpCols + threadIdx.y;
+  const int theta = angle0 + blockIdx.z;
+  if (iu >= g.cols || iv >= g.rows) return;
+  float W;
+  const float total = fp_ray_total(params[theta], columns, ws, g, iv, iu, theta, W);
   float* out = sino + ((size_t)iv * g.nangles + theta) * g.cols + iu;
   if (additive)
     *out += total;
   else
     *out = total;
+}
+
+// ---------------------------------------------------------------- batched SIRT
+// One launch over all jobs' (row block, column block, angle) tiles. Epilogue:
+// residual = W * (R * (y - A x)), which is what the plain recipe computes with
+// separate operations (y - A(x), times R, then the backprojector's W pass).
+__global__ void __launch_bounds__(kFpRows* kFpCols)
+    fp_sirt_batch_kernel(const SirtJobDev* __restrict__ jobs,
+                         const long long* __restrict__ prefix, int n_jobs) {
+  const long long b = blockIdx.x;
+  const int j = find_job(prefix, n_jobs, b);
+  const SirtJobDev& job = jobs[j];
+  const DeviceGeometry& g = job.g;
+  long long local = b - prefix[j];
+  const int rb = int(local % job.fp_row_blocks);
+  local /= job.fp_row_blocks;
+  const int cb = int(local % job.fp_col_blocks);
+  const int theta = int(local / job.fp_col_blocks);
+  const int iv = rb * kFpRows + threadIdx.x;
+  const int iu = cb * kFpCols + threadIdx.y;
+  if (iu >= g.cols || iv >= g.rows) return;
+  float W;
+  const float total = fp_ray_total(job.params[theta], job.columns, job.fp_ws, g, iv, iu, theta, W);
+  const size_t idx = ((size_t)iv * g.nangles + theta) * g.cols + iu;
+  const float r = __fmul_rn(__fsub_rn(__ldg(job.y + idx), total), __ldg(job.R + idx));
+  job.res[idx] = __fmul_rn(W, r);
+}
+
+// Layout copies of all jobs: blockIdx.y selects the (job, permutation) segment.
+__global__ void fp_layout_batch_kernel(const LayoutSegDev* __restrict__ segs) {
+  const LayoutSegDev& s = segs[blockIdx.y];
+  const long long n_ap = s.n_a + 2 * kPad, n_bp = s.n_b + 2 * kPad;
+  const long long total = (long long)s.n_d * n_ap * n_bp;
+  for (long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x; idx < total;
+       idx += (long long)gridDim.x * blockDim.x) {
+    const long long jp = idx % n_bp, rest = idx / n_bp;
+    const long long ip = rest % n_ap, k = rest / n_ap;
+    const long long i = ip - kPad, jj = jp - kPad;
+    float v = 0.0f;
+    if (i >= 0 && i < s.n_a && jj >= 0 && jj < s.n_b)
+      v = __ldg(s.vol + k * s.s_d + i * s.s_a + jj * s.s_b);
+    s.out[idx] = v;
+  }
 }
 
 }  // namespace
@@ -141,6 +198,18 @@ int launch_fp(const tsgb_projector* p, const float* vol, float* sino, bool addit
     fp_ray_kernel<<<grid, block, 0, stream>>>(p->d_params, p->d_columns, workspace, sino, g, a0,
                                               additive ? 1 : 0);
   }
+  return int(cudaGetLastError());
+}
+
+int launch_sirt_fp_batch(const SirtBatchDev& b, void* stream_) {
+  cudaStream_t stream = static_cast<cudaStream_t>(stream_);
+  if (b.n_segs > 0) {
+    const dim3 grid(unsigned(b.seg_grid_x), unsigned(b.n_segs));
+    fp_layout_batch_kernel<<<grid, 256, 0, stream>>>(b.segs);
+  }
+  if (b.fp_blocks > 0)
+    fp_sirt_batch_kernel<<<unsigned(b.fp_blocks), dim3(kFpRows, kFpCols), 0, stream>>>(
+        b.jobs, b.fp_prefix, b.n_jobs);
   return int(cudaGetLastError());
 }
 

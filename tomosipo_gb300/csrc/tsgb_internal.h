@@ -122,4 +122,11 @@ int launch_bp_matched(const tsgb_projector* p, float* vol, const float* sino, bo
 int launch_bp_bilinear(const tsgb_projector* p, float* vol, const float* sino, bool additive,
                        void* stream);
 
+// Batched SIRT (batch.cu builds the tables; fp.cu / bp.cu launch).
+struct SirtBatchDev;
+int launch_sirt_fp_batch(const SirtBatchDev& b, void* stream);
+int launch_sirt_bp_batch(const SirtBatchDev& b, void* stream);
+constexpr int kBpRunZ = 16;  // voxels along z per matched-backprojection thread
+constexpr int kBpTileX = 32, kBpTileY = 4, kFpTileRows = 32, kFpTileCols = 8;
+
 }  // namespace tsgb
