@@ -214,24 +214,132 @@ def run_reference(args, rank, world):
 
 
 # --------------------------------------------------------------------------- GPU arm
-def ellipsoid_phantom_gpu(torch, device, n=20, seed=2):
-    """Sum of ``n`` seeded random ellipsoids (densities U[0.1, 1]) on [-1, 1]^3."""
+def phantom_gpu(torch, device, n, count=8, seed=0):
+    """Sum of ``count`` seeded ellipsoids on an n^3 grid (densities U[0.1, 1])."""
     g = torch.Generator(device="cpu").manual_seed(seed)
-    ax = torch.linspace(-1, 1, N, device=device)
-    yy, xx = ax[None, :, None], ax[None, None, :]
-    x = torch.zeros((N, N, N), device=device)
-    params = []
-    for _ in range(n):
+    ax = torch.linspace(-1, 1, n, device=device)
+    x = torch.zeros((n, n, n), device=device)
+    for _ in range(count):
         c = (torch.rand(3, generator=g) - 0.5).tolist()
         r = (torch.rand(3, generator=g) * 0.35 + 0.1).tolist()
         rho = float(torch.rand(1, generator=g)) * 0.9 + 0.1
-        params.append((c, r, rho))
-    for z0 in range(0, N, 64):  # z slabs keep temporaries small
-        zz = ax[z0:z0 + 64, None, None]
-        for c, r, rho in params:
-            m = ((zz - c[0]) / r[0]) ** 2 + ((yy - c[1]) / r[1]) ** 2 + ((xx - c[2]) / r[2]) ** 2
+        for z0 in range(0, n, 64):
+            zz = ax[z0:z0 + 64, None, None]
+            m = (((zz - c[0]) / r[0]) ** 2 + ((ax[None, :, None] - c[1]) / r[1]) ** 2
+                 + ((ax[None, None, :] - c[2]) / r[2]) ** 2)
             x[z0:z0 + 64] += rho * (m <= 1)
     return x
+
+
+def noisy_projection(torch, A, x, seed):
+    """y = A(x) + N(0, 0.01 max(A(x))) (seeded)."""
+    y = A(x)
+    g = torch.Generator(device="cpu").manual_seed(seed)
+    return y + 0.01 * float(y.max()) * torch.randn(y.shape, generator=g).to(y.device)
+
+
+def bench_batched_sirt(torch, ts, device, n_jobs=64, iterations=30, seed=3):
+    """64 independent jobs (64^3..256^3, parallel or cone, 60-720 angles, detector
+    side x 1.5 side, noisy data): batched SIRT vs looping the plain operator."""
+    from tomosipo_gb300.sirt import BatchedSirt, sirt
+
+    rng = np.random.default_rng(seed)
+    jobs, updates = [], 0
+    for i in range(n_jobs):
+        n = int(rng.choice([64, 96, 128, 192, 256]))
+        cone = bool(rng.random() < 0.5)
+        angles = int(rng.integers(60, 721))
+        vg = ts.volume(shape=n, size=1)
+        pg = (ts.cone(angles=angles, shape=(n, 3 * n // 2), size=np.sqrt(2), cone_angle=0.5) if cone
+              else ts.parallel(angles=angles, shape=(n, 3 * n // 2), size=(1, 1.5)))
+        A = ts.operator(vg, pg)
+        y = noisy_projection(torch, A, phantom_gpu(torch, device, n, seed=seed * 1000 + i), i)
+        jobs.append((A, y))
+        updates += 2 * n ** 3 * angles * iterations
+    torch.cuda.synchronize()
+    # warm both paths once on the smallest job
+    small = min(jobs, key=lambda j: j[1].numel())
+    sirt(small[0], small[1], 1)
+    BatchedSirt([small]).run(1)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for A, y in jobs:
+        sirt(A, y, iterations)
+    torch.cuda.synchronize()
+    t_plain = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    b = BatchedSirt(jobs)
+    b.run(iterations, graph=True)
+    torch.cuda.synchronize()
+    t_batch = time.perf_counter() - t0
+    b.close()
+    return {
+        "config": f"{n_jobs} jobs, sides from {{64,96,128,192,256}}, parallel/cone 50/50, "
+                  f"60-720 angles, {iterations} iterations, y = A(x) + N(0, 0.01 max) (seed {seed}); "
+                  "times include computing R and C",
+        "solves_per_s": n_jobs / t_batch,
+        "plain_loop_solves_per_s": n_jobs / t_plain,
+        "speedup_vs_plain_loop": t_plain / t_batch,
+        "batched_s": t_batch,
+        "plain_loop_s": t_plain,
+        "gups": updates / t_batch / 1e9,
+    }
+
+
+def helical_cone_vec(ts, n, angles, rows, cols, rng, jitter_voxels=0.5):
+    """Helical cone_vec around z for an n^3 unit-cube volume: source/detector at
+    2 sqrt2 from the axis (the detector through it), detector sqrt2 x sqrt2*cols/rows
+    wide, 1.5 turns rising 0.5 per turn, per-angle source and detector jitter
+    N(0, jitter_voxels voxel)."""
+    turns, pitch, dist = 1.5, 0.5, 2 * np.sqrt(2)
+    t = np.linspace(0, 2 * np.pi * turns, angles, endpoint=False)
+    rise = pitch * (t / (2 * np.pi) - turns / 2)
+    c, s = np.cos(t), np.sin(t)
+    vox = 1.0 / n
+    src = np.stack([rise, -c * dist, s * dist], 1) + rng.normal(0, jitter_voxels * vox, (angles, 3))
+    det = np.stack([rise, 0 * t, 0 * t], 1) + rng.normal(0, jitter_voxels * vox, (angles, 3))
+    sv = np.sqrt(2) / rows
+    su = np.sqrt(2) * (cols / rows) / cols
+    dv = np.stack([np.full(angles, sv), 0 * t, 0 * t], 1)
+    du = np.stack([0 * t, s * su, c * su], 1)
+    return ts.cone_vec(shape=(rows, cols), src_pos=src, det_pos=det, det_v=dv, det_u=du)
+
+
+def bench_serving(torch, ts, device, n_requests=8, rate=20.0, iterations=20, seed=5):
+    """Serving loop over Poisson-arrival SIRT requests on helical cone_vec scans."""
+    from tomosipo_gb300.serving import Request, SirtServer, latency_stats
+
+    rng = np.random.default_rng(seed)
+    arrivals = np.cumsum(rng.exponential(1.0 / rate, n_requests))
+    reqs, updates = [], 0
+    for i in range(n_requests):
+        n = int(rng.choice([128, 256, 384, 512]))
+        angles = int(rng.integers(256, 1025))
+        rows, cols = n, min(3 * n // 2, 768)
+        pg = helical_cone_vec(ts, n, angles, rows, cols, rng)
+        A = ts.operator(ts.volume(shape=n, size=1), pg)
+        y = noisy_projection(torch, A, phantom_gpu(torch, device, n, seed=seed * 1000 + i), i)
+        reqs.append(Request(i, A, y, iterations, float(arrivals[i])))
+        updates += 2 * n ** 3 * angles * iterations
+    torch.cuda.synchronize()
+    server = SirtServer()
+    t0 = time.perf_counter()
+    res = server.run(reqs)
+    wall = time.perf_counter() - t0
+    st = latency_stats(res)
+    return {
+        "config": f"{n_requests} requests, Poisson arrivals {rate}/s, sides from "
+                  "{128,256,384,512}, 256-1024 angles, helical cone_vec (1.5 turns, pitch 0.5) "
+                  f"with N(0, 0.5 voxel) source/detector jitter, detector side x min(1.5 side, 768), "
+                  f"{iterations} iterations, admission by free HBM (seed {seed})",
+        "p50_latency_s": st.get("p50_s"),
+        "p99_latency_s": st.get("p99_s"),
+        "solves_per_s": st.get("solves_per_s"),
+        "completed": st["completed"],
+        "max_concurrent_jobs": server.max_concurrent,
+        "steps": server.steps,
+        "gups": updates / wall / 1e9,
+    }
 
 
 def run_ours(args, rank, world, local_rank):
@@ -247,7 +355,7 @@ def run_ours(args, rank, world, local_rank):
     torch.cuda.set_device(device)
     vg, pg = workload_geometry(ts)
     A = ts.operator(vg, pg)
-    x = ellipsoid_phantom_gpu(torch, device)
+    x = phantom_gpu(torch, device, N, count=20, seed=2)
     y = torch.empty(A.range_shape, device=device)
     v = torch.empty(A.domain_shape, device=device)
     stats = A.projector.stats(device.index)
@@ -348,6 +456,10 @@ def run_ours(args, rank, world, local_rank):
                 traffic = json.load(f).get("bp_matched_bytes_per_launch_512")
         except (OSError, ValueError):
             traffic = None
+    batched = serving = None
+    if not args.no_sirt:
+        batched = bench_batched_sirt(torch, ts, device, n_jobs=args.sirt_jobs)
+        serving = bench_serving(torch, ts, device, n_requests=args.serve_requests)
     cpu = None
     if world == 1 and not args.no_cpu_baseline:
         gups, info = cpu_baseline_sample()
@@ -383,6 +495,8 @@ def run_ours(args, rank, world, local_rank):
         },
         "cpu_baseline": cpu,
         "e2e": e2e,
+        "batched_sirt": batched,
+        "serving": serving,
         "gpu_launches": args.steps * (stats["fp_launches"] + stats["bp_matched_launches"]),
         "clocks": clock_info,
         "plan": stats,
@@ -399,6 +513,9 @@ def main():
     p.add_argument("--impl", choices=["ours", "reference"], default="ours")
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--no-sirt", action="store_true", help="skip the batched SIRT and serving parts")
+    p.add_argument("--sirt-jobs", type=int, default=64)
+    p.add_argument("--serve-requests", type=int, default=8)
     p.add_argument("--workload", choices=sorted(WORKLOADS), default="headline",
                    help="headline = the metric's 512^3/1024 workload; c2 = 256^3/360 (profiling)")
     args = p.parse_args()

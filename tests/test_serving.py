@@ -1,0 +1,132 @@
+"""Host logic of the continuous-batching SIRT server, with a fake engine and a
+fake clock (CPU): admission by memory, joining mid-run, rejection, failure
+isolation, cancellation and latency statistics."""
+import pytest
+
+from tomosipo_gb300.serving import Request, SirtServer, latency_stats
+
+
+class FakeClock:
+    def __init__(self):
+        self.t = 0.0
+
+    def __call__(self):
+        return self.t
+
+    def sleep(self, dt):
+        self.t += max(dt, 1e-3)
+
+
+class FakeEngine:
+    """Each step takes `step_time`; a job's state counts its iterations."""
+
+    def __init__(self, clock, sizes, step_time=1.0, fail_ids=()):
+        self.clock, self.sizes, self.step_time = clock, sizes, step_time
+        self.fail_ids = set(fail_ids)
+        self.batches = []
+
+    def job_bytes(self, req):
+        return self.sizes[req.id]
+
+    def admit(self, req):
+        if req.id in self.fail_ids:
+            raise RuntimeError("geometry not supported")
+        return {"id": req.id, "iters": 0}
+
+    def build(self, states):
+        self.batches.append(sorted(s["id"] for s in states))
+        return list(states)
+
+    def step(self, batch):
+        for s in batch:
+            s["iters"] += 1
+        self.clock.t += self.step_time
+
+    def result(self, state):
+        return state["iters"]
+
+    def release(self, batch):
+        pass
+
+
+def _server(sizes, budget, **kw):
+    clock = FakeClock()
+    eng = FakeEngine(clock, sizes, **{k: v for k, v in kw.items() if k in ("step_time", "fail_ids")})
+    srv = SirtServer(engine=eng, memory_budget=budget,
+                     max_active=kw.get("max_active", 64))
+    return clock, eng, srv
+
+
+def test_all_jobs_complete_with_their_iterations():
+    clock, eng, srv = _server({0: 10, 1: 10, 2: 10}, 100)
+    reqs = [Request(i, None, None, iterations=3 + i, arrival=0.0) for i in range(3)]
+    res = srv.run(reqs, clock=clock, sleep=clock.sleep)
+    assert [r.status for r in res] == ["done"] * 3
+    assert [r.x for r in res] == [3, 4, 5]
+    assert srv.max_concurrent == 3
+
+
+def test_admission_waits_for_memory_and_joins_mid_run():
+    # budget fits two jobs; job 2 waits until one finishes, then joins the running job
+    clock, eng, srv = _server({0: 40, 1: 40, 2: 40}, 100)
+    reqs = [Request(0, None, None, 2, 0.0), Request(1, None, None, 5, 0.0), Request(2, None, None, 2, 0.0)]
+    res = srv.run(reqs, clock=clock, sleep=clock.sleep)
+    assert all(r.status == "done" for r in res)
+    assert eng.batches[0] == [0, 1]
+    assert [1, 2] in eng.batches  # continuous batching: 2 runs alongside 1
+    assert res[2].admitted >= res[0].finished
+    assert res[2].x == 2
+
+
+def test_late_arrival_joins_running_batch():
+    clock, eng, srv = _server({0: 10, 1: 10}, 100)
+    reqs = [Request(0, None, None, 10, 0.0), Request(1, None, None, 3, 2.5)]
+    res = srv.run(reqs, clock=clock, sleep=clock.sleep)
+    assert eng.batches == [[0], [0, 1], [0]]
+    assert res[1].admitted < res[0].finished
+    assert res[1].latency == pytest.approx(res[1].finished - 2.5)
+
+
+def test_oversized_request_is_rejected_others_served():
+    clock, eng, srv = _server({0: 500, 1: 10}, 100)
+    res = srv.run([Request(0, None, None, 2, 0.0), Request(1, None, None, 2, 0.0)],
+                  clock=clock, sleep=clock.sleep)
+    assert res[0].status == "rejected" and "budget" in res[0].error
+    assert res[1].status == "done"
+
+
+def test_failed_setup_is_isolated():
+    clock, eng, srv = _server({0: 10, 1: 10, 2: 10}, 100, fail_ids={1})
+    res = srv.run([Request(i, None, None, 2, 0.0) for i in range(3)], clock=clock, sleep=clock.sleep)
+    assert [r.status for r in res] == ["done", "failed", "done"]
+    assert "geometry" in res[1].error
+    assert srv.used == 0
+
+
+def test_cancellation_of_waiting_and_running():
+    clock, eng, srv = _server({0: 60, 1: 60, 2: 10}, 100)
+    srv.cancel(1)
+    reqs = [Request(0, None, None, 4, 0.0), Request(1, None, None, 4, 0.0), Request(2, None, None, 4, 0.0)]
+    res = srv.run(reqs, clock=clock, sleep=clock.sleep)
+    assert [r.status for r in res] == ["done", "cancelled", "done"]
+    clock2, eng2, srv2 = _server({0: 10}, 100)
+
+    class CancelMidway(FakeEngine):
+        def step(self, batch):
+            super().step(batch)
+            if batch[0]["iters"] == 2:
+                srv2.cancel(0)
+
+    eng2.__class__ = CancelMidway
+    res2 = srv2.run([Request(0, None, None, 10, 0.0)], clock=clock2, sleep=clock2.sleep)
+    assert res2[0].status == "cancelled" and srv2.used == 0
+
+
+def test_latency_stats():
+    clock, eng, srv = _server({i: 1 for i in range(10)}, 100, max_active=2)
+    reqs = [Request(i, None, None, 1, 0.0) for i in range(10)]
+    st = latency_stats(srv.run(reqs, clock=clock, sleep=clock.sleep))
+    assert st["completed"] == 10
+    assert st["p50_s"] == pytest.approx(3.0, abs=0.6)
+    assert st["p99_s"] == pytest.approx(5.0, abs=0.1)
+    assert st["solves_per_s"] == pytest.approx(2.0)

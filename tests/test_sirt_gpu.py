@@ -90,3 +90,22 @@ def test_batched_rejects_tilted_detectors(dev):
     y = torch.zeros(A.range_shape, device=dev)
     with pytest.raises(RuntimeError, match="separable"):
         BatchedSirt([(A, y)])
+
+
+def test_server_results_same_alone_and_in_mix(dev):
+    """Continuous batching: jobs arriving over time, different sizes; each result
+    equals the same request run alone (and the plain SIRT loop)."""
+    from tomosipo_gb300.serving import Request, SirtServer
+
+    jobs = [_job(dev, 32, True, 40, 11), _job(dev, 48, True, 64, 12), _job(dev, 40, False, 50, 13)]
+    reqs = [Request(i, A, y, iterations=4 + 2 * i, arrival=0.02 * i) for i, (A, y, _) in enumerate(jobs)]
+    res = SirtServer(memory_budget=2 << 30).run(reqs)
+    assert all(r.status == "done" for r in res)
+    for r, (A, y, _) in zip(res, jobs):
+        alone = SirtServer(memory_budget=2 << 30).run([Request(0, A, y, r_iters(reqs, r.id))])[0]
+        assert torch.equal(r.x, alone.x)
+        assert torch.equal(r.x, sirt(A, y, r_iters(reqs, r.id)))
+
+
+def r_iters(reqs, rid):
+    return next(q.iterations for q in reqs if q.id == rid)

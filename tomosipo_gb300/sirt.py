@@ -53,6 +53,75 @@ def sirt(A, y, num_iterations=10, x_init=None, R=None, C=None):
     return x
 
 
+class SirtJobState:
+    """Device buffers of one SIRT job: x, y, R, C, residual and FP workspace."""
+
+    def __init__(self, A, y, x_init=None, device=None):
+        device = y.device if device is None else device
+        if device.type != "cuda":
+            raise ValueError("batched SIRT runs on CUDA tensors")
+        self.A = A
+        self.device = device
+        with torch.cuda.device(device):
+            self.y = y.to(device=device, dtype=torch.float32).contiguous()
+            self.R, self.C = preconditioners(A, device)
+            self.x = (torch.zeros(A.domain_shape, device=device) if x_init is None
+                      else x_init.to(device, torch.float32).contiguous().clone())
+            self.res = torch.empty(A.range_shape, device=device)
+            nbytes = A.projector.workspace_bytes(device.index, True)
+            self.ws = torch.empty(max(nbytes, 4) // 4, device=device)
+
+    @staticmethod
+    def device_bytes(A):
+        """Device memory a job holds: x, C (volume) and y, R, residual (sinogram) plus workspace."""
+        vol = 4 * int(torch.Size(A.domain_shape).numel())
+        sino = 4 * int(torch.Size(A.range_shape).numel())
+        stats_ws = A.projector.stats(torch.cuda.current_device())["fp_workspace_bytes"]
+        return 2 * vol + 3 * sino + stats_ws
+
+
+class NativeBatch:
+    """Native job table over a list of SirtJobState (rebuilt when jobs change)."""
+
+    def __init__(self, states):
+        if not states:
+            raise ValueError("a batch needs at least one job")
+        self.states = list(states)
+        self.device = states[0].device
+        lib = _native.load()
+        table = (_native.SirtJob * len(states))()
+        for i, st in enumerate(states):
+            if st.device != self.device:
+                raise ValueError("all jobs must be on the same device")
+            t = table[i]
+            t.projector = st.A.projector.handle(self.device.index)
+            t.vol, t.sino, t.R, t.C = st.x.data_ptr(), st.y.data_ptr(), st.R.data_ptr(), st.C.data_ptr()
+            t.residual, t.fp_workspace = st.res.data_ptr(), st.ws.data_ptr()
+        out = ctypes.c_void_p()
+        with torch.cuda.device(self.device):
+            _native.check(lib.tsgb_sirt_batch_create(table, len(states), ctypes.byref(out)),
+                          "tsgb_sirt_batch_create")
+        self._batch = out.value
+
+    def step(self, iterations=1):
+        lib = _native.load()
+        with torch.cuda.device(self.device):
+            stream = torch.cuda.current_stream(self.device).cuda_stream
+            _native.check(lib.tsgb_sirt_batch_iterate(self._batch, int(iterations), stream),
+                          "tsgb_sirt_batch_iterate")
+
+    def close(self):
+        if getattr(self, "_batch", None):
+            _native.load().tsgb_sirt_batch_destroy(self._batch)
+            self._batch = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
 class BatchedSirt:
     """SIRT for many independent jobs, advanced together.
 
@@ -70,44 +139,26 @@ class BatchedSirt:
         self.device = jobs[0][1].device
         if self.device.type != "cuda":
             raise ValueError("BatchedSirt runs on CUDA tensors")
-        lib = _native.load()
-        self._keep = []
-        self.x, self.R, self.C = [], [], []
-        table = (_native.SirtJob * len(jobs))()
-        with torch.cuda.device(self.device):
-            for i, job in enumerate(jobs):
-                A, y = job[0], job[1]
-                x0 = job[2] if len(job) > 2 else None
-                if y.device != self.device:
-                    raise ValueError("all jobs must be on the same device")
-                y = y.to(torch.float32).contiguous()
-                R, C = preconditioners(A, self.device)
-                x = (torch.zeros(A.domain_shape, device=self.device) if x0 is None
-                     else x0.to(self.device, torch.float32).contiguous().clone())
-                res = torch.empty(A.range_shape, device=self.device)
-                nbytes = A.projector.workspace_bytes(self.device.index, True)
-                ws = torch.empty(max(nbytes, 4) // 4, device=self.device)
-                self._keep += [A, y, res, ws]
-                self.x.append(x)
-                self.R.append(R)
-                self.C.append(C)
-                t = table[i]
-                t.projector = A.projector.handle(self.device.index)
-                t.vol, t.sino, t.R, t.C = x.data_ptr(), y.data_ptr(), R.data_ptr(), C.data_ptr()
-                t.residual, t.fp_workspace = res.data_ptr(), ws.data_ptr()
-            out = ctypes.c_void_p()
-            _native.check(lib.tsgb_sirt_batch_create(table, len(jobs), ctypes.byref(out)),
-                          "tsgb_sirt_batch_create")
-        self._batch = out.value
+        self.states = [SirtJobState(j[0], j[1], j[2] if len(j) > 2 else None, self.device)
+                       for j in jobs]
+        self._native = NativeBatch(self.states)
         self._graph = None
+
+    @property
+    def x(self):
+        return [st.x for st in self.states]
+
+    @property
+    def R(self):
+        return [st.R for st in self.states]
+
+    @property
+    def C(self):
+        return [st.C for st in self.states]
 
     def step(self, iterations=1):
         """Queue ``iterations`` iterations on the current stream."""
-        lib = _native.load()
-        with torch.cuda.device(self.device):
-            stream = torch.cuda.current_stream(self.device).cuda_stream
-            _native.check(lib.tsgb_sirt_batch_iterate(self._batch, int(iterations), stream),
-                          "tsgb_sirt_batch_iterate")
+        self._native.step(iterations)
 
     def _capture(self):
         g = torch.cuda.CUDAGraph()
@@ -128,12 +179,4 @@ class BatchedSirt:
         return self.x
 
     def close(self):
-        if getattr(self, "_batch", None):
-            _native.load().tsgb_sirt_batch_destroy(self._batch)
-            self._batch = None
-
-    def __del__(self):
-        try:
-            self.close()
-        except Exception:
-            pass
+        self._native.close()
