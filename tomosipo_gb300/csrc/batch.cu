@@ -63,7 +63,11 @@ int tsgb_sirt_batch_create(const tsgb_sirt_job* jobs, int32_t n_jobs, tsgb_sirt_
     d.columns = p->d_columns;
     d.sep_angles = p->d_sep_angles;
     d.n_sep = p->n_separable_bp;
-    d.wide = (size_t)g.rows * g.nangles * g.cols >= (size_t(1) << 31) ? 1 : 0;
+    d.wide = (size_t)(g.rows + 2 * tsgb::kRowPad) * g.nangles * g.cols >= (size_t(1) << 31) ? 1 : 0;
+    if (d.wide)
+      return bfail(TSGB_ERR_INVALID, "job " + std::to_string(i) +
+                                         " has a sinogram of 2^31 floats or more; run it with the "
+                                         "plain operator");
     d.g = g;
     d.vol = J.vol;
     d.y = J.sino;

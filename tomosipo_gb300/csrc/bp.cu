@@ -23,6 +23,8 @@
 // magnification squared).
 #include <cuda_runtime.h>
 
+#include <type_traits>
+
 #include "device_common.cuh"
 
 namespace tsgb {
@@ -49,29 +51,27 @@ __global__ void __launch_bounds__(256)
   const size_t idx = ((size_t)iv * g.nangles + theta) * g.cols + iu;
   float w = 0.0f;
   if (finite_ray(r) && fabsf(r.ma) <= kMaxSlope && fabsf(r.mb) <= kMaxSlope) w = ray_step(ap, r);
-  out[idx] = w * __ldg(sino + idx);
-}
-
-// Detector value y'[iv][theta][iu] through a column pointer, zero outside
-// the detector rows. Offsets are 32-bit when the sinogram has < 2^31 floats.
-template <bool kWide>
-__device__ __forceinline__ float column_value(const float* __restrict__ col, int iv, int rows,
-                                              unsigned row_stride32, size_t row_stride) {
-  if (iv < 0 || iv >= rows) return 0.0f;
-  return kWide ? __ldg(col + (size_t)iv * row_stride) : __ldg(col + (unsigned)iv * row_stride32);
+  // out has kRowPad zero rows above and below the detector
+  out[idx + (size_t)kRowPad * g.nangles * g.cols] = w * __ldg(sino + idx);
 }
 
 // Matched backprojection of the angles in `angles` for the voxel column
 // (x, y) and the kRun voxels z0 .. z0 + kRun - 1, accumulated into acc.
+// sinow is the W-weighted sinogram with kRowPad zero rows above and below the
+// detector (rows -kRowPad .. rows + kRowPad - 1), so the two-row path reads
+// without bounds tests once its row index is clamped into the padding.
+// Offsets are 32-bit unless kWide (padded sinogram of 2^31 floats or more).
 template <int kRun, bool kWide>
 __device__ __forceinline__ void bp_separable_accumulate(
     const AngleParams* __restrict__ params, const ColumnEntry* __restrict__ columns,
     const int* __restrict__ angles, int n_angles, const float* __restrict__ sinow,
     const DeviceGeometry& g, int x, int y, int z0, float (&acc)[kRun]) {
+  using Offset = typename std::conditional<kWide, long long, int>::type;
   const float xt = float(x - g.ox), yt = float(y - g.oy);
   const float zt0 = float(z0 - g.oz);
-  const size_t row_stride = (size_t)g.nangles * g.cols;
-  const unsigned row_stride32 = (unsigned)row_stride;
+  const Offset rs = Offset(g.nangles) * g.cols;  // row stride
+  const float* __restrict__ sinow0 = sinow + (long long)kRowPad * rs;  // row 0
+  const float vmin = float(-kRowPad - g.ov), vmax = float(g.rows - g.ov);
   const float4* __restrict__ col4 = reinterpret_cast<const float4*>(columns);
 #pragma unroll
   for (int j = 0; j < kRun; ++j) acc[j] = 0.0f;
@@ -92,7 +92,7 @@ __device__ __forceinline__ void bp_separable_accumulate(
     const float u2 = __fdividef(fmaf(th, ap.e[0], -A0), fmaf(-th, ap.e[1], A1));
     const int iu_lo = max(0, (int)floorf(clamp_coord(fminf(u1, u2))) + 1 + g.ou);
     const int iu_hi = min(g.cols - 1, (int)ceilf(clamp_coord(fmaxf(u1, u2))) - 1 + g.ou);
-    const float* __restrict__ sino_theta = sinow + (size_t)theta * g.cols;
+    const float* __restrict__ sino_theta = sinow0 + (size_t)theta * g.cols;
     for (int iu = iu_lo; iu <= iu_hi; ++iu) {
       const size_t ci = ((size_t)theta * g.cols + iu) * 2;
       const float4 c0 = __ldg(col4 + ci);      // Xa, ma, P, Q
@@ -110,14 +110,14 @@ __device__ __forceinline__ void bp_separable_accumulate(
 #pragma unroll
         for (int j = 0; j < kRun; ++j) {
           const float vs = fmaf(float(j), inv, vs0);
-          const float v0 = floorf(clamp_coord(vs));
+          // Rows outside [-kRowPad, rows] hold zeros either way: clamping keeps
+          // both reads inside the padding (NaN clamps to the low end).
+          const float v0 = fminf(fmaxf(floorf(vs), vmin), vmax);
           const float Bj = B - (zt0 + float(j));
           const float w0 = tent(fmaf(v0, Sl, Bj));
           const float w1 = tent(fmaf(v0 + 1.0f, Sl, Bj));
-          const int iv0 = (int)v0 + g.ov;
-          const float y0 = column_value<kWide>(col, iv0, g.rows, row_stride32, row_stride);
-          const float y1 = column_value<kWide>(col, iv0 + 1, g.rows, row_stride32, row_stride);
-          acc[j] = fmaf(h, fmaf(w0, y0, w1 * y1), acc[j]);
+          const float* p = col + Offset((int)v0 + g.ov) * rs;
+          acc[j] = fmaf(h, fmaf(w0, __ldg(p), w1 * __ldg(p + rs)), acc[j]);
         }
       } else {
 #pragma unroll
@@ -129,7 +129,7 @@ __device__ __forceinline__ void bp_separable_accumulate(
           float s = 0.0f;
           for (int iv = iv_lo; iv <= iv_hi; ++iv) {
             const float w = tent(fmaf(float(iv - g.ov), Sl, Bj));
-            s = fmaf(w, column_value<kWide>(col, iv, g.rows, row_stride32, row_stride), s);
+            s = fmaf(w, __ldg(col + Offset(iv) * rs), s);
           }
           acc[j] = fmaf(h, s, acc[j]);
         }
@@ -184,12 +184,9 @@ __global__ void __launch_bounds__(kBpX* kBpY)
   const int z0 = zb * kRun;
   if (x >= g.nx || y >= g.ny) return;
   float acc[kRun];
-  if (job.wide)
-    bp_separable_accumulate<kRun, true>(job.params, job.columns, job.sep_angles, job.n_sep,
-                                        job.res, g, x, y, z0, acc);
-  else
-    bp_separable_accumulate<kRun, false>(job.params, job.columns, job.sep_angles, job.n_sep,
-                                         job.res, g, x, y, z0, acc);
+  // batch creation rejects jobs whose padded sinogram needs 64-bit offsets
+  bp_separable_accumulate<kRun, false>(job.params, job.columns, job.sep_angles, job.n_sep,
+                                       job.res, g, x, y, z0, acc);
 #pragma unroll
   for (int j = 0; j < kRun; ++j) {
     const int z = z0 + j;
@@ -247,7 +244,7 @@ __global__ void __launch_bounds__(128)
     const int iu_hi = min(g.cols - 1, (int)ceilf(clamp_coord(umax)) - 1 + g.ou);
     const int iv_lo = max(0, (int)floorf(clamp_coord(vmin)) + 1 + g.ov);
     const int iv_hi = min(g.rows - 1, (int)ceilf(clamp_coord(vmax)) - 1 + g.ov);
-    const float* base = sinow + (size_t)theta * g.cols;
+    const float* base = sinow + ((size_t)kRowPad * g.nangles + theta) * g.cols;
     for (int iv = iv_lo; iv <= iv_hi; ++iv) {
       const float vt = float(iv - g.ov);
       for (int iu = iu_lo; iu <= iu_hi; ++iu) {
@@ -367,11 +364,17 @@ int launch_bp_matched(const tsgb_projector* p, float* vol, const float* sino, bo
                                                    workspace + (size_t)a0 * g.cols, g);
     }
   }
+  {
+    // zero the kRowPad rows above and below the detector
+    const size_t pad = (size_t)kRowPad * g.nangles * g.cols * sizeof(float);
+    cudaMemsetAsync(workspace, 0, pad, stream);
+    cudaMemsetAsync(workspace + (size_t)(kRowPad + g.rows) * g.nangles * g.cols, 0, pad, stream);
+  }
   bool written = false;
   if (p->n_separable_bp > 0) {
     const dim3 block(kBpX, kBpY);
     const dim3 grid((g.nx + kBpX - 1) / kBpX, (g.ny + kBpY - 1) / kBpY, (g.nz + kRunZ - 1) / kRunZ);
-    const bool wide = (size_t)g.rows * g.nangles * g.cols >= (size_t(1) << 31);
+    const bool wide = (size_t)(g.rows + 2 * kRowPad) * g.nangles * g.cols >= (size_t(1) << 31);
     if (wide)
       bp_separable_kernel<kRunZ, true><<<grid, block, 0, stream>>>(
           p->d_params, p->d_columns, p->d_sep_angles, p->n_separable_bp, workspace, vol, g,

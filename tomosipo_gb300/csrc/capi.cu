@@ -122,7 +122,7 @@ int64_t tsgb_bp_workspace_bytes(const tsgb_projector* p, int32_t bp_kind) {
   if (!p) return fail(TSGB_ERR_INVALID, "projector is NULL");
   if (bp_kind == TSGB_BP_BILINEAR) return 0;
   if (bp_kind != TSGB_BP_MATCHED) return fail(TSGB_ERR_INVALID, "unknown bp_kind");
-  return int64_t(p->g.rows) * p->g.nangles * p->g.cols * int64_t(sizeof(float));
+  return int64_t(p->g.rows + 2 * tsgb::kRowPad) * p->g.nangles * p->g.cols * int64_t(sizeof(float));
 }
 
 int tsgb_projector_shapes(const tsgb_projector* p, int64_t vol_shape[3], int64_t sino_shape[3]) {

@@ -154,7 +154,8 @@ __global__ void __launch_bounds__(kFpRows* kFpCols)
   const float total = fp_ray_total(job.params[theta], job.columns, job.fp_ws, g, iv, iu, theta, W);
   const size_t idx = ((size_t)iv * g.nangles + theta) * g.cols + iu;
   const float r = __fmul_rn(__fsub_rn(__ldg(job.y + idx), total), __ldg(job.R + idx));
-  job.res[idx] = __fmul_rn(W, r);
+  // res has kRowPad zero rows above and below the detector (never written)
+  job.res[idx + (size_t)kRowPad * g.nangles * g.cols] = __fmul_rn(W, r);
 }
 
 // Layout copies of all jobs: blockIdx.y selects the (job, permutation) segment.

@@ -28,6 +28,7 @@
 namespace tsgb {
 
 constexpr int kPad = 2;        // zero padding of the forward-projection volume copies
+constexpr int kRowPad = 2;     // zero detector rows above and below the weighted sinogram
 constexpr int kMaxLayouts = 6; // axis permutations (d, a, b)
 
 // Per-angle parameters, read uniformly by all threads of a block.

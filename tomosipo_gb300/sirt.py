@@ -67,7 +67,9 @@ class SirtJobState:
             self.R, self.C = preconditioners(A, device)
             self.x = (torch.zeros(A.domain_shape, device=device) if x_init is None
                       else x_init.to(device, torch.float32).contiguous().clone())
-            self.res = torch.empty(A.range_shape, device=device)
+            rows, angles, cols = A.range_shape
+            # two zero detector rows above and below (read as padding by the BP)
+            self.res = torch.zeros((rows + 4) * angles * cols, device=device)
             nbytes = A.projector.workspace_bytes(device.index, True)
             self.ws = torch.empty(max(nbytes, 4) // 4, device=device)
 
@@ -75,9 +77,10 @@ class SirtJobState:
     def device_bytes(A):
         """Device memory a job holds: x, C (volume) and y, R, residual (sinogram) plus workspace."""
         vol = 4 * int(torch.Size(A.domain_shape).numel())
-        sino = 4 * int(torch.Size(A.range_shape).numel())
+        rows, angles, cols = A.range_shape
+        sino = 4 * rows * angles * cols
         stats_ws = A.projector.stats(torch.cuda.current_device())["fp_workspace_bytes"]
-        return 2 * vol + 3 * sino + stats_ws
+        return 2 * vol + 3 * sino + 16 * angles * cols + stats_ws
 
 
 class NativeBatch:
