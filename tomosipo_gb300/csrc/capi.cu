@@ -181,7 +181,7 @@ int tsgb_direct_bp(tsgb_projector* p, float* vol, const float* sino, int32_t add
 int tsgb_projector_stats(const tsgb_projector* p, int64_t* out, int32_t n) {
   if (!p || !out || n < 0 || n > 8) return fail(TSGB_ERR_INVALID, "bad stats arguments");
   const int64_t chunks = (p->g.nangles + 65534) / 65535;
-  const int64_t fp_launches = int64_t(p->layouts.size()) + chunks;
+  const int64_t fp_launches = int64_t(p->layouts.size()) + (p->g.nangles + 2 * 65535 - 1) / (2 * 65535);
   const int64_t bp_launches =
       chunks + (p->n_separable_bp > 0 ? 1 : 0) + ((p->n_general_bp > 0 || p->n_separable_bp == 0) ? 1 : 0);
   const int64_t vals[8] = {int64_t(p->layouts.size()),

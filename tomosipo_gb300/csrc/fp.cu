@@ -76,59 +76,140 @@ __device__ __forceinline__ float bilinear_sample(const float* __restrict__ base,
   return fmaf(fa, right - left, left);
 }
 
-// Ray sum of pixel (iv, iu) at angle theta, already scaled by the plane step.
-// W receives the plane step the transpose weights this ray with (0 for rays
-// that are not sampled), exactly as bp_weight_kernel computes it.
+// A ray prepared for sampling: its coefficients, plane range and copy base.
+struct RayWalk {
+  Ray r;
+  const float* base;  // anchored voxel (0, 0, 0) of the angle's padded copy
+  int k0, k1;         // planes to sample (k0 > k1: none)
+  int stride_d, stride_a;
+  float W;            // plane step (0 if the ray is not sampled)
+};
+
+__device__ __forceinline__ RayWalk prepare_ray(const AngleParams& ap,
+                                               const ColumnEntry* __restrict__ columns,
+                                               const float* __restrict__ ws,
+                                               const DeviceGeometry& g, int iv, int iu,
+                                               int theta) {
+  RayWalk w;
+  const float vt = float(iv - g.ov);
+  w.r = ap.separable ? ray_column(columns[(size_t)theta * g.cols + iu], vt)
+                     : ray_general(ap, float(iu - g.ou), vt);
+  w.k0 = 1;
+  w.k1 = 0;
+  w.W = 0.0f;
+  w.stride_d = ap.stride_d;
+  w.stride_a = ap.stride_a;
+  w.base = ws + ap.ws_offset + (long long)ap.o_d * ap.stride_d +
+           (long long)(ap.o_a + kPad) * ap.stride_a + (ap.o_b + kPad);
+  if (finite_ray(w.r) && fabsf(w.r.ma) <= kMaxSlope && fabsf(w.r.mb) <= kMaxSlope) {
+    w.W = ray_step(ap, w.r);
+    float klo = float(-ap.o_d), khi = float(ap.n_d - 1 - ap.o_d);
+    clip_planes(w.r.Xa, w.r.ma, float(-1 - ap.o_a), float(ap.n_a - ap.o_a), klo, khi);
+    clip_planes(w.r.Xb, w.r.mb, float(-1 - ap.o_b), float(ap.n_b - ap.o_b), klo, khi);
+    if (klo <= khi) {
+      w.k0 = (int)ceilf(klo);
+      w.k1 = (int)floorf(khi);
+    }
+  }
+  return w;
+}
+
+__device__ __forceinline__ float sample(const RayWalk& w, int k) {
+  return bilinear_sample(w.base, w.r, k, w.stride_d, w.stride_a);
+}
+
+// Samples of planes k0..k1 are summed into two partial sums by the parity of
+// k (even planes into e, odd into o), in increasing k, so a ray's result does
+// not depend on how its planes are scheduled against another ray's.
+__device__ __forceinline__ void walk(const RayWalk& w, int k0, int k1, float& e, float& o) {
+  int k = k0;
+  if (k <= k1 && (k & 1)) o += sample(w, k++);
+  for (; k < k1; k += 2) {
+    e += sample(w, k);
+    o += sample(w, k + 1);
+  }
+  if (k == k1) e += sample(w, k);
+}
+
+// Ray sum (scaled by the plane step) of pixel (iv, iu) at angle theta. W
+// receives the plane step the transpose weights this ray with (0 for rays that
+// are not sampled), exactly as bp_weight_kernel computes it.
 __device__ __forceinline__ float fp_ray_total(const AngleParams& ap,
                                               const ColumnEntry* __restrict__ columns,
                                               const float* __restrict__ ws,
                                               const DeviceGeometry& g, int iv, int iu, int theta,
                                               float& W) {
-  const float vt = float(iv - g.ov);
-  const Ray r = ap.separable ? ray_column(columns[(size_t)theta * g.cols + iu], vt)
-                             : ray_general(ap, float(iu - g.ou), vt);
-  float total = 0.0f;
-  W = 0.0f;
-  if (finite_ray(r) && fabsf(r.ma) <= kMaxSlope && fabsf(r.mb) <= kMaxSlope) {
-    W = ray_step(ap, r);
-    const int o_d = ap.o_d, o_a = ap.o_a, o_b = ap.o_b;
-    const int stride_d = ap.stride_d, stride_a = ap.stride_a;
-    float klo = float(-o_d), khi = float(ap.n_d - 1 - o_d);
-    clip_planes(r.Xa, r.ma, float(-1 - o_a), float(ap.n_a - o_a), klo, khi);
-    clip_planes(r.Xb, r.mb, float(-1 - o_b), float(ap.n_b - o_b), klo, khi);
-    if (klo <= khi) {
-      const int k0 = (int)ceilf(klo), k1 = (int)floorf(khi);
-      // base points at anchored voxel (0, 0, 0) of this copy
-      const float* base = ws + ap.ws_offset + (long long)o_d * stride_d +
-                          (long long)(o_a + kPad) * stride_a + (o_b + kPad);
-      float acc0 = 0.0f, acc1 = 0.0f;
-      int k = k0;
-      for (; k < k1; k += 2) {
-        acc0 += bilinear_sample(base, r, k, stride_d, stride_a);
-        acc1 += bilinear_sample(base, r, k + 1, stride_d, stride_a);
-      }
-      if (k == k1) acc0 += bilinear_sample(base, r, k, stride_d, stride_a);
-      total = (acc0 + acc1) * W;
-    }
-  }
-  return total;
+  const RayWalk w = prepare_ray(ap, columns, ws, g, iv, iu, theta);
+  W = w.W;
+  float e = 0.0f, o = 0.0f;
+  walk(w, w.k0, w.k1, e, o);
+  return w.k0 <= w.k1 ? (e + o) * w.W : 0.0f;
 }
 
+// Two adjacent angles of one pixel. When both use the same volume copy their
+// planes are walked together, so the second ray's taps (near the first's)
+// hit lines the first just brought into L1. Results equal fp_ray_total's.
+__device__ __forceinline__ void fp_ray_pair(const AngleParams& apa, const AngleParams& apb,
+                                            const ColumnEntry* __restrict__ columns,
+                                            const float* __restrict__ ws,
+                                            const DeviceGeometry& g, int iv, int iu, int theta,
+                                            float& ta, float& tb) {
+  const RayWalk a = prepare_ray(apa, columns, ws, g, iv, iu, theta);
+  const RayWalk b = prepare_ray(apb, columns, ws, g, iv, iu, theta + 1);
+  float ea = 0.0f, oa = 0.0f, eb = 0.0f, ob = 0.0f;
+  const int lo = max(a.k0, b.k0), hi = min(a.k1, b.k1);
+  if (apa.layout == apb.layout && lo <= hi) {
+    walk(a, a.k0, lo - 1, ea, oa);
+    walk(b, b.k0, lo - 1, eb, ob);
+    int k = lo;
+    if (k & 1) {
+      oa += sample(a, k);
+      ob += sample(b, k);
+      ++k;
+    }
+    for (; k < hi; k += 2) {
+      ea += sample(a, k);
+      eb += sample(b, k);
+      oa += sample(a, k + 1);
+      ob += sample(b, k + 1);
+    }
+    if (k == hi) {
+      ea += sample(a, k);
+      eb += sample(b, k);
+    }
+    walk(a, hi + 1, a.k1, ea, oa);
+    walk(b, hi + 1, b.k1, eb, ob);
+  } else {
+    walk(a, a.k0, a.k1, ea, oa);
+    walk(b, b.k0, b.k1, eb, ob);
+  }
+  ta = a.k0 <= a.k1 ? (ea + oa) * a.W : 0.0f;
+  tb = b.k0 <= b.k1 ? (eb + ob) * b.W : 0.0f;
+}
+
+// One thread per pixel and pair of adjacent angles (blockIdx.z = pair).
 __global__ void __launch_bounds__(kFpRows* kFpCols)
     fp_ray_kernel(const AngleParams* __restrict__ params, const ColumnEntry* __restrict__ columns,
                   const float* __restrict__ ws, float* __restrict__ sino, DeviceGeometry g,
                   int angle0, int additive) {
   const int iv = blockIdx.x * kFpRows + threadIdx.x;
   const int iu = blockIdx.y * kFpCols + threadIdx.y;
-  const int theta = angle0 + blockIdx.z;
+  const int theta = angle0 + 2 * blockIdx.z;
   if (iu >= g.cols || iv >= g.rows) return;
-  float W;
-  const float total = fp_ray_total(params[theta], columns, ws, g, iv, iu, theta, W);
-  float* out = sino + ((size_t)iv * g.nangles + theta) * g.cols + iu;
-  if (additive)
-    *out += total;
+  float ta, tb = 0.0f, W;
+  const bool pair = theta + 1 < g.nangles;
+  if (pair)
+    fp_ray_pair(params[theta], params[theta + 1], columns, ws, g, iv, iu, theta, ta, tb);
   else
-    *out = total;
+    ta = fp_ray_total(params[theta], columns, ws, g, iv, iu, theta, W);
+  float* out = sino + ((size_t)iv * g.nangles + theta) * g.cols + iu;
+  if (additive) {
+    out[0] += ta;
+    if (pair) out[g.cols] += tb;
+  } else {
+    out[0] = ta;
+    if (pair) out[g.cols] = tb;
+  }
 }
 
 // ---------------------------------------------------------------- batched SIRT
@@ -193,9 +274,9 @@ int launch_fp(const tsgb_projector* p, const float* vol, float* sino, bool addit
                                                   vstride[L.a], vstride[L.b]);
   }
   const dim3 block(kFpRows, kFpCols);
-  for (int a0 = 0; a0 < g.nangles; a0 += 65535) {
-    const int n = g.nangles - a0 < 65535 ? g.nangles - a0 : 65535;
-    const dim3 grid((g.rows + kFpRows - 1) / kFpRows, (g.cols + kFpCols - 1) / kFpCols, n);
+  for (int a0 = 0; a0 < g.nangles; a0 += 2 * 65535) {
+    const int n = g.nangles - a0 < 2 * 65535 ? g.nangles - a0 : 2 * 65535;
+    const dim3 grid((g.rows + kFpRows - 1) / kFpRows, (g.cols + kFpCols - 1) / kFpCols, (n + 1) / 2);
     fp_ray_kernel<<<grid, block, 0, stream>>>(p->d_params, p->d_columns, workspace, sino, g, a0,
                                               additive ? 1 : 0);
   }
