@@ -291,8 +291,9 @@ __device__ __forceinline__ float detector_bilinear(const float* __restrict__ bas
 }
 
 __global__ void __launch_bounds__(kBpX* kBpY)
-    bp_bilinear_kernel(const AngleParams* __restrict__ params, const float* __restrict__ sino,
-                       float* __restrict__ vol, DeviceGeometry g, int additive) {
+    bp_bilinear_kernel(const AngleParams* __restrict__ params, const int* __restrict__ angles,
+                       int n_angles, const float* __restrict__ sino, float* __restrict__ vol,
+                       DeviceGeometry g, int additive) {
   const int x = blockIdx.x * kBpX + threadIdx.x;
   const int y = blockIdx.y * kBpY + threadIdx.y;
   const int z0 = blockIdx.z * kRunZBil;
@@ -304,7 +305,8 @@ __global__ void __launch_bounds__(kBpX* kBpY)
   float acc[kRunZBil];
 #pragma unroll
   for (int j = 0; j < kRunZBil; ++j) acc[j] = 0.0f;
-  for (int theta = 0; theta < g.nangles; ++theta) {
+  for (int n = 0; n < n_angles; ++n) {
+    const int theta = __ldg(angles + n);
     const AngleParams& ap = params[theta];
     const float* base = sino + (size_t)theta * g.cols;
     for (int sz = 0; sz < ss; ++sz)
@@ -343,6 +345,101 @@ __global__ void __launch_bounds__(kBpX* kBpY)
         *out += acc[j] * norm;
       else
         *out = acc[j] * norm;
+    }
+  }
+}
+
+// Copy the sinogram into a layout with kRowPad zero rows above and below and
+// kColPad zero columns left and right of the detector.
+__global__ void bp_bilinear_prep_kernel(const float* __restrict__ sino, float* __restrict__ out,
+                                        DeviceGeometry g) {
+  const long long cp = g.cols + 2 * kColPad, rp = g.rows + 2 * kRowPad;
+  const long long total = rp * g.nangles * cp;
+  for (long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x; idx < total;
+       idx += (long long)gridDim.x * blockDim.x) {
+    const long long c = idx % cp, rest = idx / cp;
+    const long long t = rest % g.nangles, r = rest / g.nangles;
+    const long long iu = c - kColPad, iv = r - kRowPad;
+    float v = 0.0f;
+    if (iu >= 0 && iu < g.cols && iv >= 0 && iv < g.rows)
+      v = __ldg(sino + ((size_t)iv * g.nangles + t) * g.cols + iu);
+    out[idx] = v;
+  }
+}
+
+// Bilinear backprojection of angles whose projection keeps u and the
+// projective denominator constant along z (det_v along z). A thread owns a
+// voxel column (x, y) and kRun voxels along z: per angle it projects the
+// column once (detector column pair, 1/w, the distance weight's horizontal
+// part), then per voxel only steps the detector row. sinop is the padded copy
+// made by bp_bilinear_prep_kernel, so no read needs a bounds test once its
+// indices are clamped into the padding (positions outside the detector read
+// zeros, as bilinear interpolation with a zero border does).
+template <int kRun>
+__global__ void __launch_bounds__(kBpX* kBpY)
+    bp_bilinear_z_kernel(const AngleParams* __restrict__ params, const int* __restrict__ angles,
+                         int n_angles, const float* __restrict__ sinop, float* __restrict__ vol,
+                         DeviceGeometry g, int additive) {
+  const int x = blockIdx.x * kBpX + threadIdx.x;
+  const int y = blockIdx.y * kBpY + threadIdx.y;
+  const int z0 = blockIdx.z * kRun;
+  if (x >= g.nx || y >= g.ny) return;
+  const bool cone = g.kind == TSGB_CONE;
+  const float xt = float(x - g.ox), yt = float(y - g.oy), zt0 = float(z0 - g.oz);
+  const int cp = g.cols + 2 * kColPad;
+  const int rs = g.nangles * cp;  // padded row stride (padded copy < 2^31 floats)
+  const float* __restrict__ base0 = sinop + kRowPad * rs + kColPad;
+  const float umin = float(-kColPad - g.ou), umax = float(g.cols - g.ou);
+  const float vmin = float(-kRowPad - g.ov), vmax = float(g.rows - g.ov);
+  float acc[kRun];
+#pragma unroll
+  for (int j = 0; j < kRun; ++j) acc[j] = 0.0f;
+  for (int n = 0; n < n_angles; ++n) {
+    const int theta = __ldg(angles + n);
+    const AngleParams& ap = params[theta];
+    const float nw = fmaf(ap.pw[1], yt, fmaf(ap.pw[2], xt, ap.pw[3]));
+    if (!(nw > 0.0f)) continue;  // the column lies behind the source
+    const float inw = 1.0f / nw;
+    const float ut = fmaf(ap.pu[1], yt, fmaf(ap.pu[2], xt, ap.pu[3])) * inw;
+    const float fu0 = floorf(ut);
+    const float fu = ut - fu0;
+    const float* __restrict__ colp = base0 + theta * cp + ((int)fminf(fmaxf(fu0, umin), umax) + g.ou);
+    const float nvc = fmaf(ap.pv[1], yt, fmaf(ap.pv[2], xt, ap.pv[3]));
+    float K = ap.bil_scale, dxy2 = 0.0f;
+    if (cone) {
+      K *= inw * inw * inw;
+      const float dx = (xt - ap.src[2]) * g.vs[2], dy = (yt - ap.src[1]) * g.vs[1];
+      dxy2 = fmaf(dx, dx, dy * dy);
+    }
+#pragma unroll
+    for (int j = 0; j < kRun; ++j) {
+      const float zt = zt0 + float(j);
+      const float vt = fmaf(ap.pv[0], zt, nvc) * inw;
+      const float fv0 = floorf(vt);
+      const float fv = vt - fv0;
+      const float* p = colp + ((int)fminf(fmaxf(fv0, vmin), vmax) + g.ov) * rs;
+      const float v00 = __ldg(p), v01 = __ldg(p + 1), v10 = __ldg(p + rs), v11 = __ldg(p + rs + 1);
+      const float top = fmaf(fu, v01 - v00, v00);
+      const float bot = fmaf(fu, v11 - v10, v10);
+      const float val = fmaf(fv, bot - top, top);
+      float c = K;
+      if (cone) {
+        const float dz = (zt - ap.src[0]) * g.vs[0];
+        const float l2 = fmaf(dz, dz, dxy2);
+        c *= l2 * rsqrtf(l2);
+      }
+      acc[j] = fmaf(c, val, acc[j]);
+    }
+  }
+#pragma unroll
+  for (int j = 0; j < kRun; ++j) {
+    const int z = z0 + j;
+    if (z < g.nz) {
+      float* out = vol + ((size_t)z * g.ny + y) * g.nx + x;
+      if (additive)
+        *out += acc[j];
+      else
+        *out = acc[j];
     }
   }
 }
@@ -404,12 +501,28 @@ int launch_sirt_bp_batch(const SirtBatchDev& b, void* stream_) {
 }
 
 int launch_bp_bilinear(const tsgb_projector* p, float* vol, const float* sino, bool additive,
-                       void* stream_) {
+                       float* workspace, void* stream_) {
   cudaStream_t stream = static_cast<cudaStream_t>(stream_);
   const DeviceGeometry& g = p->g;
   const dim3 block(kBpX, kBpY);
-  const dim3 grid((g.nx + kBpX - 1) / kBpX, (g.ny + kBpY - 1) / kBpY, (g.nz + kRunZBil - 1) / kRunZBil);
-  bp_bilinear_kernel<<<grid, block, 0, stream>>>(p->d_params, sino, vol, g, additive ? 1 : 0);
+  bool written = false;
+  if (p->n_bil_fast > 0) {
+    const long long total = (long long)(g.rows + 2 * kRowPad) * g.nangles * (g.cols + 2 * kColPad);
+    const long long blocks = (total + 255) / 256;
+    bp_bilinear_prep_kernel<<<int(blocks < 152LL * 64 ? blocks : 152LL * 64), 256, 0, stream>>>(
+        sino, workspace, g);
+    const dim3 grid((g.nx + kBpX - 1) / kBpX, (g.ny + kBpY - 1) / kBpY, (g.nz + kRunZ - 1) / kRunZ);
+    bp_bilinear_z_kernel<kRunZ><<<grid, block, 0, stream>>>(p->d_params, p->d_bil_fast,
+                                                            p->n_bil_fast, workspace, vol, g,
+                                                            additive ? 1 : 0);
+    written = true;
+  }
+  if (p->n_bil_slow > 0 || !written) {
+    const dim3 grid((g.nx + kBpX - 1) / kBpX, (g.ny + kBpY - 1) / kBpY,
+                    (g.nz + kRunZBil - 1) / kRunZBil);
+    bp_bilinear_kernel<<<grid, block, 0, stream>>>(p->d_params, p->d_bil_slow, p->n_bil_slow, sino,
+                                                   vol, g, (additive || written) ? 1 : 0);
+  }
   return int(cudaGetLastError());
 }
 

@@ -27,6 +27,10 @@ void free_device(tsgb_projector* p) {
   if (p->d_columns) cudaFree(p->d_columns);
   if (p->d_sep_angles) cudaFree(p->d_sep_angles);
   if (p->d_gen_angles) cudaFree(p->d_gen_angles);
+  if (p->d_bil_fast) cudaFree(p->d_bil_fast);
+  if (p->d_bil_slow) cudaFree(p->d_bil_slow);
+  p->d_bil_fast = nullptr;
+  p->d_bil_slow = nullptr;
   p->d_params = nullptr;
   p->d_columns = nullptr;
   p->d_sep_angles = nullptr;
@@ -70,9 +74,9 @@ int tsgb_projector_create(const tsgb_volume_desc* vol, const tsgb_projection_des
   tsgb_projector* p = new (std::nothrow) tsgb_projector();
   if (!p) return fail(TSGB_ERR_INVALID, "host allocation failed");
   std::vector<tsgb::ColumnEntry> columns;
-  std::vector<int> sep, gen;
+  std::vector<int> sep, gen, bfast, bslow;
   std::string err = tsgb::build_plan(vol, proj, voxel_supersampling, detector_supersampling, p,
-                                     &columns, &sep, &gen);
+                                     &columns, &sep, &gen, &bfast, &bslow);
   if (!err.empty()) {
     delete p;
     return fail(TSGB_ERR_INVALID, err);
@@ -92,6 +96,8 @@ int tsgb_projector_create(const tsgb_volume_desc* vol, const tsgb_projection_des
   if (e == cudaSuccess) e = upload(&p->d_columns, columns);
   if (e == cudaSuccess) e = upload(&p->d_sep_angles, sep);
   if (e == cudaSuccess) e = upload(&p->d_gen_angles, gen);
+  if (e == cudaSuccess) e = upload(&p->d_bil_fast, bfast);
+  if (e == cudaSuccess) e = upload(&p->d_bil_slow, bslow);
   if (e != cudaSuccess) {
     free_device(p);
     delete p;
@@ -120,7 +126,10 @@ int64_t tsgb_fp_workspace_bytes(const tsgb_projector* p) {
 
 int64_t tsgb_bp_workspace_bytes(const tsgb_projector* p, int32_t bp_kind) {
   if (!p) return fail(TSGB_ERR_INVALID, "projector is NULL");
-  if (bp_kind == TSGB_BP_BILINEAR) return 0;
+  if (bp_kind == TSGB_BP_BILINEAR)
+    return p->n_bil_fast > 0 ? int64_t(p->g.rows + 2 * tsgb::kRowPad) * p->g.nangles *
+                                   (p->g.cols + 2 * tsgb::kColPad) * int64_t(sizeof(float))
+                             : 0;
   if (bp_kind != TSGB_BP_MATCHED) return fail(TSGB_ERR_INVALID, "unknown bp_kind");
   return int64_t(p->g.rows + 2 * tsgb::kRowPad) * p->g.nangles * p->g.cols * int64_t(sizeof(float));
 }
@@ -173,7 +182,8 @@ int tsgb_direct_bp(tsgb_projector* p, float* vol, const float* sino, int32_t add
     e = cudaError_t(tsgb::launch_bp_matched(p, vol, sino, additive != 0,
                                             static_cast<float*>(workspace), stream));
   else
-    e = cudaError_t(tsgb::launch_bp_bilinear(p, vol, sino, additive != 0, stream));
+    e = cudaError_t(tsgb::launch_bp_bilinear(p, vol, sino, additive != 0,
+                                             static_cast<float*>(workspace), stream));
   if (e != cudaSuccess) return cuda_fail(e, "backprojection launch");
   return TSGB_OK;
 }
@@ -189,7 +199,8 @@ int tsgb_projector_stats(const tsgb_projector* p, int64_t* out, int32_t n) {
                            p->n_general_bp,
                            fp_launches,
                            bp_launches,
-                           1,
+                           (p->n_bil_fast > 0 ? 2 : 0) +
+                               ((p->n_bil_slow > 0 || p->n_bil_fast == 0) ? 1 : 0),
                            tsgb_fp_workspace_bytes(p),
                            tsgb_bp_workspace_bytes(p, TSGB_BP_MATCHED)};
   for (int i = 0; i < n; ++i) out[i] = vals[i];

@@ -52,7 +52,8 @@ bool finite3(const V3& v) {
 std::string build_plan(const tsgb_volume_desc* vol, const tsgb_projection_desc* proj,
                        int voxel_ss, int det_ss, tsgb_projector* p,
                        std::vector<ColumnEntry>* columns, std::vector<int>* sep_angles,
-                       std::vector<int>* gen_angles) {
+                       std::vector<int>* gen_angles, std::vector<int>* bil_fast,
+                       std::vector<int>* bil_slow) {
   if (!vol || !proj || !proj->vectors) return "null geometry descriptor";
   if (proj->kind != TSGB_PARALLEL && proj->kind != TSGB_CONE)
     return "projection kind must be TSGB_PARALLEL or TSGB_CONE";
@@ -104,6 +105,8 @@ std::string build_plan(const tsgb_volume_desc* vol, const tsgb_projection_desc* 
   columns->assign(size_t(g.nangles) * g.cols, ColumnEntry{});
   sep_angles->clear();
   gen_angles->clear();
+  bil_fast->clear();
+  bil_slow->clear();
 
   for (int t = 0; t < g.nangles; ++t) {
     const double* row = proj->vectors + 12 * size_t(t);
@@ -225,6 +228,12 @@ std::string build_plan(const tsgb_volume_desc* vol, const tsgb_projection_desc* 
       ap.pv[i] = float(pv[i]);
       ap.pw[i] = float(pw[i]);
     }
+    // Exact zeros when det_v runs along z (V = (v, 0, 0)): then u and the
+    // projective denominator are constant along a voxel column in z.
+    const bool pad_fits = int64_t(g.rows + 2 * kRowPad) * g.nangles * (g.cols + 2 * kColPad) <
+                          (int64_t(1) << 31);
+    ap.bil_zflat = (pad_fits && voxel_ss == 1 && pu[0] == 0.0 && pw[0] == 0.0) ? 1 : 0;
+    (ap.bil_zflat ? bil_fast : bil_slow)->push_back(t);
     for (int i = 0; i < 3; ++i) ap.src[i] = float(S[i]);
 
     // Forward-projection volume copy for this (d, a, b).
@@ -289,6 +298,8 @@ std::string build_plan(const tsgb_volume_desc* vol, const tsgb_projection_desc* 
   p->fp_workspace_floats = off;
   p->n_general_bp = int(gen_angles->size());
   p->n_separable_bp = int(sep_angles->size());
+  p->n_bil_fast = int(bil_fast->size());
+  p->n_bil_slow = int(bil_slow->size());
   return std::string();
 }
 

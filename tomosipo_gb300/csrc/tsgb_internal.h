@@ -29,6 +29,7 @@ namespace tsgb {
 
 constexpr int kPad = 2;        // zero padding of the forward-projection volume copies
 constexpr int kRowPad = 2;     // zero detector rows above and below the weighted sinogram
+constexpr int kColPad = 2;     // zero detector columns left and right (bilinear BP copy)
 constexpr int kMaxLayouts = 6; // axis permutations (d, a, b)
 
 // Per-angle parameters, read uniformly by all threads of a block.
@@ -37,7 +38,8 @@ struct alignas(16) AngleParams {
   int separable;     // det_v has no d or a component: column table is valid
   int layout;        // index of the padded volume copy used by the forward projector
   int bp_general;    // 1: backprojected by the general kernel (else separable kernel)
-  int pad0, pad1;
+  int bil_zflat;     // projection's u numerator and denominator do not depend on z
+  int pad1;
   // Ray coefficients, functions of anchored pixel coordinates (ut, vt):
   //   den = e0 + e1 ut + e2 vt,  X_a = (ca . [1,ut,vt]) / den,  m_a = (ma . [1,ut,vt]) / den
   // and the same for b. Parallel beams have den = 1.
@@ -96,10 +98,14 @@ struct tsgb_projector {
   int64_t fp_workspace_floats = 0;
   int n_general_bp = 0;         // angles handled by the general BP kernel
   int n_separable_bp = 0;       // angles handled by the separable BP kernel
+  int n_bil_fast = 0;           // bilinear BP: angles for the z-flat kernel
+  int n_bil_slow = 0;           // bilinear BP: angles for the general kernel
   tsgb::AngleParams* d_params = nullptr;
   tsgb::ColumnEntry* d_columns = nullptr;  // [nangles][cols]
   int* d_sep_angles = nullptr;             // angle ids for the separable BP kernel
   int* d_gen_angles = nullptr;             // angle ids for the general BP kernel
+  int* d_bil_fast = nullptr;               // angle ids, bilinear z-flat kernel
+  int* d_bil_slow = nullptr;               // angle ids, bilinear general kernel
 };
 
 namespace tsgb {
@@ -110,7 +116,8 @@ namespace tsgb {
 std::string build_plan(const tsgb_volume_desc* vol, const tsgb_projection_desc* proj,
                        int voxel_ss, int det_ss, tsgb_projector* p,
                        std::vector<ColumnEntry>* columns,
-                       std::vector<int>* sep_angles, std::vector<int>* gen_angles);
+                       std::vector<int>* sep_angles, std::vector<int>* gen_angles,
+                       std::vector<int>* bil_fast, std::vector<int>* bil_slow);
 
 // Sets the calling thread's message returned by tsgb_last_error (capi.cu).
 void set_last_error(const std::string& msg);
@@ -121,7 +128,7 @@ int launch_fp(const tsgb_projector* p, const float* vol, float* sino, bool addit
 int launch_bp_matched(const tsgb_projector* p, float* vol, const float* sino, bool additive,
                       float* workspace, void* stream);
 int launch_bp_bilinear(const tsgb_projector* p, float* vol, const float* sino, bool additive,
-                       void* stream);
+                       float* workspace, void* stream);
 
 // Batched SIRT (batch.cu builds the tables; fp.cu / bp.cu launch).
 struct SirtBatchDev;
