@@ -342,6 +342,78 @@ def bench_serving(torch, ts, device, n_requests=8, rate=20.0, iterations=20, see
     }
 
 
+def bench_lpd(torch, ts, device, batch=8, n=128, angles=128, iterations=10, channels=32,
+              steps=3, warmup=2):
+    """One training step (forward, backward, SGD update) of the unrolled learned
+    primal-dual: cone 128^3, 128 angles, detector 128 x 192, bf16 convolutions,
+    fp32 projector, iterations recomputed (checkpointed) in the backward pass."""
+    from tomosipo_gb300.lpd import LearnedPrimalDual3d
+
+    vg = ts.volume(shape=n, size=1)
+    pg = ts.cone(angles=angles, shape=(n, 3 * n // 2), size=np.sqrt(2), cone_angle=0.5)
+    A = ts.operator(vg, pg)
+    torch.manual_seed(0)
+    net = LearnedPrimalDual3d(A, n_iters=iterations, channels=channels).to(device)
+    opt = torch.optim.SGD(net.parameters(), lr=1e-4)
+    x = torch.stack([phantom_gpu(torch, device, n, count=8, seed=40 + i) for i in range(batch)])[:, None]
+    g = torch.stack([A(x[i, 0]) for i in range(batch)])[:, None]
+
+    def step():
+        opt.zero_grad(set_to_none=True)
+        loss = (net(g) - x).square().mean()
+        loss.backward()
+        opt.step()
+        return loss
+
+    for _ in range(warmup):
+        step()
+    torch.cuda.synchronize()
+    torch.cuda.reset_peak_memory_stats(device)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(steps):
+        loss = step()
+    e1.record()
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / steps
+    # projector work per step: forward 2 x (FP + BP) per iteration (recomputed),
+    # backward one BP and one FP per iteration, each over the batch
+    updates = iterations * 3 * 2 * batch * n ** 3 * angles
+    return {
+        "config": f"batch {batch}, cone {n}^3, {angles} angles, detector {n}x{3 * n // 2}, "
+                  f"{iterations} unrolled iterations, 3-layer 3D CNN with {channels} channels, "
+                  "bf16 convolutions, fp32 projector, checkpointed iterations, SGD step",
+        "ms_per_step": ms,
+        "samples_per_s": batch * 1e3 / ms,
+        "projector_gups_in_step": updates / (ms / 1e3) / 1e9,
+        "peak_mem_gb": torch.cuda.max_memory_allocated(device) / 1e9,
+        "loss": float(loss.detach()),
+    }
+
+
+def bench_bilinear_pair(torch, ts, device, x, steps):
+    """FP + the bilinear (ASTRA-style) BP on the headline workload."""
+    vg, pg = workload_geometry(ts)
+    A = ts.operator(vg, pg, backprojector="bilinear")
+    y = torch.empty(A.range_shape, device=device)
+    v = torch.empty(A.domain_shape, device=device)
+    A(x, out=y)
+    A.T(y, out=v)
+    torch.cuda.synchronize()
+    ev = [[torch.cuda.Event(enable_timing=True) for _ in range(3)] for _ in range(steps)]
+    for e in ev:
+        e[0].record()
+        A(x, out=y)
+        e[1].record()
+        A.T(y, out=v)
+        e[2].record()
+    torch.cuda.synchronize()
+    fp = statistics.mean(e[0].elapsed_time(e[1]) for e in ev)
+    bp = statistics.mean(e[1].elapsed_time(e[2]) for e in ev)
+    return {"fp_ms": fp, "bp_bilinear_ms": bp,
+            "gups": 2 * N ** 3 * ANGLES / ((fp + bp) / 1e3) / 1e9}
+
+
 def run_ours(args, rank, world, local_rank):
     import torch
     import torch.distributed as dist
@@ -456,7 +528,11 @@ def run_ours(args, rank, world, local_rank):
                 traffic = json.load(f).get("bp_matched_bytes_per_launch_512")
         except (OSError, ValueError):
             traffic = None
-    batched = serving = None
+    batched = serving = lpd = bilinear = None
+    if not args.no_bilinear:
+        bilinear = bench_bilinear_pair(torch, ts, device, x, args.steps)
+    if not args.no_lpd:
+        lpd = bench_lpd(torch, ts, device)
     if not args.no_sirt:
         batched = bench_batched_sirt(torch, ts, device, n_jobs=args.sirt_jobs)
         serving = bench_serving(torch, ts, device, n_requests=args.serve_requests)
@@ -497,6 +573,8 @@ def run_ours(args, rank, world, local_rank):
         "e2e": e2e,
         "batched_sirt": batched,
         "serving": serving,
+        "learned_primal_dual": lpd,
+        "fp_plus_bilinear_bp": bilinear,
         "gpu_launches": args.steps * (stats["fp_launches"] + stats["bp_matched_launches"]),
         "clocks": clock_info,
         "plan": stats,
@@ -514,6 +592,8 @@ def main():
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-sirt", action="store_true", help="skip the batched SIRT and serving parts")
+    p.add_argument("--no-lpd", action="store_true", help="skip the learned primal-dual step")
+    p.add_argument("--no-bilinear", action="store_true", help="skip the FP + bilinear BP pair")
     p.add_argument("--sirt-jobs", type=int, default=64)
     p.add_argument("--serve-requests", type=int, default=8)
     p.add_argument("--workload", choices=sorted(WORKLOADS), default="headline",
