@@ -141,6 +141,26 @@ int tsgb_sirt_batch_iterate(tsgb_sirt_batch* b, int32_t iterations, void* stream
 /* Free a batch's tables (not the jobs' buffers). */
 int tsgb_sirt_batch_destroy(tsgb_sirt_batch* b);
 
+/* Launch schedule of a projector's forward projection (the order of its
+ * independent tiles; a tile is 32 detector rows x 8 columns of one pair of
+ * adjacent angles). The detector is cut into patches of fp_patch_rows x
+ * fp_patch_cols tiles and the angles into groups of fp_group_pairs pairs;
+ * a group's tiles over one patch run together, so the volume slab their rays
+ * cross is read from HBM once and reused from L2 across the group's angles.
+ * Any values >= 1 give bit-identical results. Defaults are set at creation;
+ * the Python autotuner times candidates and sets the fastest. Used by
+ * tsgb_direct_fp and by the batched SIRT forward pass. No counterpart in the
+ * reference (ASTRA's launch shapes are fixed). */
+typedef struct {
+  int32_t fp_patch_rows;  /* tiles of 32 detector rows per patch (>= 1) */
+  int32_t fp_patch_cols;  /* tiles of 8 detector columns per patch (>= 1) */
+  int32_t fp_group_pairs; /* pairs of adjacent angles per group (>= 1) */
+  int32_t reserved[5];    /* must be 0 */
+} tsgb_tuning;
+
+int tsgb_projector_get_tuning(const tsgb_projector* p, tsgb_tuning* out);
+int tsgb_projector_set_tuning(tsgb_projector* p, const tsgb_tuning* t);
+
 /* Shapes the projector expects: vol (z, y, x) and sino (rows, angles, cols). */
 int tsgb_projector_shapes(const tsgb_projector* p, int64_t vol_shape[3],
                           int64_t sino_shape[3]);

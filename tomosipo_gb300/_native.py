@@ -46,6 +46,15 @@ class SirtJob(ctypes.Structure):
     ]
 
 
+class Tuning(ctypes.Structure):
+    _fields_ = [
+        ("fp_patch_rows", ctypes.c_int32),
+        ("fp_patch_cols", ctypes.c_int32),
+        ("fp_group_pairs", ctypes.c_int32),
+        ("reserved", ctypes.c_int32 * 5),
+    ]
+
+
 _lib = None
 _lock = threading.Lock()
 
@@ -85,6 +94,8 @@ SIGNATURES = {
     ),
     "tsgb_sirt_batch_iterate": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, ctypes.c_void_p]),
     "tsgb_sirt_batch_destroy": (ctypes.c_int, [ctypes.c_void_p]),
+    "tsgb_projector_get_tuning": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(Tuning)]),
+    "tsgb_projector_set_tuning": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(Tuning)]),
     "tsgb_last_error": (ctypes.c_char_p, []),
 }
 

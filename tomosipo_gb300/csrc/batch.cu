@@ -75,12 +75,13 @@ int tsgb_sirt_batch_create(const tsgb_sirt_job* jobs, int32_t n_jobs, tsgb_sirt_
     d.C = J.C;
     d.res = J.residual;
     d.fp_ws = J.fp_workspace;
-    d.fp_row_blocks = (g.rows + tsgb::kFpTileRows - 1) / tsgb::kFpTileRows;
-    d.fp_col_blocks = (g.cols + tsgb::kFpTileCols - 1) / tsgb::kFpTileCols;
+    // the job's forward tiles in its projector's order, one per angle pair
+    d.fp_sched = tsgb::fp_schedule(p, (g.nangles + 1) / 2);
     d.bp_xb = (g.nx + tsgb::kBpTileX - 1) / tsgb::kBpTileX;
     d.bp_yb = (g.ny + tsgb::kBpTileY - 1) / tsgb::kBpTileY;
     d.bp_zb = (g.nz + tsgb::kBpRunZ - 1) / tsgb::kBpRunZ;
-    fp_prefix[i + 1] = fp_prefix[i] + (long long)d.fp_row_blocks * d.fp_col_blocks * g.nangles;
+    fp_prefix[i + 1] = fp_prefix[i] + (long long)d.fp_sched.row_blocks *
+                                          d.fp_sched.col_blocks * d.fp_sched.pairs;
     bp_prefix[i + 1] = bp_prefix[i] + (long long)d.bp_xb * d.bp_yb * d.bp_zb;
     const long long vstride[3] = {(long long)g.ny * g.nx, (long long)g.nx, 1};
     for (const auto& L : p->layouts) {

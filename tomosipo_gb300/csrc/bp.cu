@@ -165,9 +165,12 @@ __global__ void __launch_bounds__(kBpX* kBpY)
 }
 
 // Batched SIRT backprojection over all jobs' voxel tiles; epilogue
-// x += C * A^T(res), rounded as the plain recipe's x += C * bp.
+// x += C * A^T(res), rounded as the plain recipe's x += C * bp. The job
+// descriptor lives in global memory rather than in the parameter bank, which
+// costs registers; 9 resident blocks per SM keep it at bp_separable_kernel's
+// 56 registers (no spills).
 template <int kRun>
-__global__ void __launch_bounds__(kBpX* kBpY)
+__global__ void __launch_bounds__(kBpX* kBpY, 9)
     bp_sirt_batch_kernel(const SirtJobDev* __restrict__ jobs, const long long* __restrict__ prefix,
                          int n_jobs) {
   const long long b = blockIdx.x;

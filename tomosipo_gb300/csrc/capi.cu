@@ -91,6 +91,7 @@ int tsgb_projector_create(const tsgb_volume_desc* vol, const tsgb_projection_des
     return fail(TSGB_ERR_INVALID,
                 "volume z extent must be <= 65535, detector rows <= 262140 and columns <= 524280");
   }
+  p->tuning = tsgb::default_tuning(p->g);
   cudaError_t e = cudaGetDevice(&p->device);
   if (e == cudaSuccess) e = upload(&p->d_params, p->host_params);
   if (e == cudaSuccess) e = upload(&p->d_columns, columns);
@@ -191,7 +192,8 @@ int tsgb_direct_bp(tsgb_projector* p, float* vol, const float* sino, int32_t add
 int tsgb_projector_stats(const tsgb_projector* p, int64_t* out, int32_t n) {
   if (!p || !out || n < 0 || n > 8) return fail(TSGB_ERR_INVALID, "bad stats arguments");
   const int64_t chunks = (p->g.nangles + 65534) / 65535;
-  const int64_t fp_launches = int64_t(p->layouts.size()) + (p->g.nangles + 2 * 65535 - 1) / (2 * 65535);
+  const int64_t chunk = tsgb::fp_angle_chunk(p->g);
+  const int64_t fp_launches = int64_t(p->layouts.size()) + (p->g.nangles + chunk - 1) / chunk;
   const int64_t bp_launches =
       chunks + (p->n_separable_bp > 0 ? 1 : 0) + ((p->n_general_bp > 0 || p->n_separable_bp == 0) ? 1 : 0);
   const int64_t vals[8] = {int64_t(p->layouts.size()),
@@ -204,6 +206,24 @@ int tsgb_projector_stats(const tsgb_projector* p, int64_t* out, int32_t n) {
                            tsgb_fp_workspace_bytes(p),
                            tsgb_bp_workspace_bytes(p, TSGB_BP_MATCHED)};
   for (int i = 0; i < n; ++i) out[i] = vals[i];
+  return TSGB_OK;
+}
+
+int tsgb_projector_get_tuning(const tsgb_projector* p, tsgb_tuning* out) {
+  g_last_error.clear();
+  if (!p || !out) return fail(TSGB_ERR_INVALID, "projector or out is NULL");
+  *out = p->tuning;
+  return TSGB_OK;
+}
+
+int tsgb_projector_set_tuning(tsgb_projector* p, const tsgb_tuning* t) {
+  g_last_error.clear();
+  if (!p || !t) return fail(TSGB_ERR_INVALID, "projector or tuning is NULL");
+  if (t->fp_patch_rows < 1 || t->fp_patch_cols < 1 || t->fp_group_pairs < 1)
+    return fail(TSGB_ERR_INVALID, "tuning values must be >= 1");
+  for (int i = 0; i < 5; ++i)
+    if (t->reserved[i] != 0) return fail(TSGB_ERR_INVALID, "reserved tuning fields must be 0");
+  p->tuning = *t;
   return TSGB_OK;
 }
 

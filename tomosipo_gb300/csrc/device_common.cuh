@@ -98,7 +98,7 @@ struct SirtJobDev {
   const float* C;     // per-voxel weights (volume-shaped)
   float* res;         // W * R * (y - A x) (sinogram-shaped)
   const float* fp_ws; // padded volume copies
-  int fp_row_blocks, fp_col_blocks;
+  FpSchedule fp_sched; // forward tile order over all of the job's angles
   int bp_xb, bp_yb, bp_zb;
 };
 
@@ -119,6 +119,34 @@ struct SirtBatchDev {
   int n_jobs, n_segs;
   long long fp_blocks, bp_blocks, seg_grid_x;
 };
+
+// Tile (row block, column block, angle pair) of linear block b under s. The
+// blocks of a group of pairs come first, inside a group the patches strip by
+// strip, inside a patch the pairs and then the tiles with row blocks fastest.
+// Only the last group, strip and patch can be smaller than the others, so
+// each level's index is a plain quotient.
+__device__ __forceinline__ void fp_schedule_tile(const FpSchedule& s, long long b, int& rb,
+                                                 int& cb, int& pair) {
+  const long long per_pair = (long long)s.row_blocks * s.col_blocks;
+  const long long full_group = per_pair * s.group_pairs;
+  const int grp = int(b / full_group);
+  b -= grp * full_group;
+  const int gsz = min(s.group_pairs, s.pairs - grp * s.group_pairs);
+  const long long full_strip = (long long)gsz * s.patch_rows * s.col_blocks;
+  const int pr = int(b / full_strip);
+  b -= pr * full_strip;
+  const int rsz = min(s.patch_rows, s.row_blocks - pr * s.patch_rows);
+  const long long full_patch = (long long)gsz * rsz * s.patch_cols;
+  const int pc = int(b / full_patch);
+  b -= pc * full_patch;
+  const int csz = min(s.patch_cols, s.col_blocks - pc * s.patch_cols);
+  const long long tiles = (long long)rsz * csz;
+  const long long q = b / tiles;
+  pair = grp * s.group_pairs + int(q);
+  const int t = int(b - q * tiles);
+  rb = pr * s.patch_rows + t % rsz;
+  cb = pc * s.patch_cols + t / rsz;
+}
 
 // Job whose block range [prefix[j], prefix[j+1]) holds block b.
 __device__ __forceinline__ int find_job(const long long* __restrict__ prefix, int n, long long b) {

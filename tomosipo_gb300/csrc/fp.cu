@@ -17,6 +17,8 @@
 //     but measured slower at 512^3 / 1024 angles, the headline size.)
 #include <cuda_runtime.h>
 
+#include <algorithm>
+
 #include "device_common.cuh"
 
 namespace tsgb {
@@ -76,133 +78,165 @@ __device__ __forceinline__ float bilinear_sample(const float* __restrict__ base,
   return fmaf(fa, right - left, left);
 }
 
-// A ray prepared for sampling: its coefficients, plane range and copy base.
-struct RayWalk {
-  Ray r;
-  const float* base;  // anchored voxel (0, 0, 0) of the angle's padded copy
-  int k0, k1;         // planes to sample (k0 > k1: none)
+// The padded volume copy an angle samples: anchored voxel (0, 0, 0) and strides.
+struct CopyView {
+  const float* base;
   int stride_d, stride_a;
-  float W;            // plane step (0 if the ray is not sampled)
 };
 
-__device__ __forceinline__ RayWalk prepare_ray(const AngleParams& ap,
-                                               const ColumnEntry* __restrict__ columns,
-                                               const float* __restrict__ ws,
-                                               const DeviceGeometry& g, int iv, int iu,
-                                               int theta) {
-  RayWalk w;
-  const float vt = float(iv - g.ov);
-  w.r = ap.separable ? ray_column(columns[(size_t)theta * g.cols + iu], vt)
-                     : ray_general(ap, float(iu - g.ou), vt);
-  w.k0 = 1;
-  w.k1 = 0;
-  w.W = 0.0f;
-  w.stride_d = ap.stride_d;
-  w.stride_a = ap.stride_a;
-  w.base = ws + ap.ws_offset + (long long)ap.o_d * ap.stride_d +
+__device__ __forceinline__ CopyView copy_view(const AngleParams& ap, const float* __restrict__ ws) {
+  CopyView v;
+  v.stride_d = ap.stride_d;
+  v.stride_a = ap.stride_a;
+  v.base = ws + ap.ws_offset + (long long)ap.o_d * ap.stride_d +
            (long long)(ap.o_a + kPad) * ap.stride_a + (ap.o_b + kPad);
-  if (finite_ray(w.r) && fabsf(w.r.ma) <= kMaxSlope && fabsf(w.r.mb) <= kMaxSlope) {
-    w.W = ray_step(ap, w.r);
-    float klo = float(-ap.o_d), khi = float(ap.n_d - 1 - ap.o_d);
-    clip_planes(w.r.Xa, w.r.ma, float(-1 - ap.o_a), float(ap.n_a - ap.o_a), klo, khi);
-    clip_planes(w.r.Xb, w.r.mb, float(-1 - ap.o_b), float(ap.n_b - ap.o_b), klo, khi);
-    if (klo <= khi) {
-      w.k0 = (int)ceilf(klo);
-      w.k1 = (int)floorf(khi);
-    }
-  }
-  return w;
+  return v;
 }
 
-__device__ __forceinline__ float sample(const RayWalk& w, int k) {
-  return bilinear_sample(w.base, w.r, k, w.stride_d, w.stride_a);
+// A ray's coefficients and the planes it samples (k0 > k1: none).
+struct RaySpan {
+  Ray r;
+  int k0, k1;
+};
+
+__device__ __forceinline__ bool ray_sampled(const Ray& r) {
+  return finite_ray(r) && fabsf(r.ma) <= kMaxSlope && fabsf(r.mb) <= kMaxSlope;
+}
+
+// Plane step the transpose weights a ray with (0 for rays that are not
+// sampled), exactly as bp_weight_kernel computes it.
+__device__ __forceinline__ float ray_weight(const AngleParams& ap, const Ray& r) {
+  return ray_sampled(r) ? ray_step(ap, r) : 0.0f;
+}
+
+__device__ __forceinline__ RaySpan prepare_span(const AngleParams& ap,
+                                                const ColumnEntry* __restrict__ columns,
+                                                const DeviceGeometry& g, int iv, int iu,
+                                                int theta) {
+  RaySpan s;
+  const float vt = float(iv - g.ov);
+  s.r = ap.separable ? ray_column(columns[(size_t)theta * g.cols + iu], vt)
+                     : ray_general(ap, float(iu - g.ou), vt);
+  s.k0 = 1;
+  s.k1 = 0;
+  if (ray_sampled(s.r)) {
+    float klo = float(-ap.o_d), khi = float(ap.n_d - 1 - ap.o_d);
+    clip_planes(s.r.Xa, s.r.ma, float(-1 - ap.o_a), float(ap.n_a - ap.o_a), klo, khi);
+    clip_planes(s.r.Xb, s.r.mb, float(-1 - ap.o_b), float(ap.n_b - ap.o_b), klo, khi);
+    if (klo <= khi) {
+      s.k0 = (int)ceilf(klo);
+      s.k1 = (int)floorf(khi);
+    }
+  }
+  return s;
+}
+
+__device__ __forceinline__ float sample(const CopyView& v, const Ray& r, int k) {
+  return bilinear_sample(v.base, r, k, v.stride_d, v.stride_a);
 }
 
 // Samples of planes k0..k1 are summed into two partial sums by the parity of
 // k (even planes into e, odd into o), in increasing k, so a ray's result does
 // not depend on how its planes are scheduled against another ray's.
-__device__ __forceinline__ void walk(const RayWalk& w, int k0, int k1, float& e, float& o) {
+__device__ __forceinline__ void walk(const CopyView& v, const Ray& r, int k0, int k1, float& e,
+                                     float& o) {
   int k = k0;
-  if (k <= k1 && (k & 1)) o += sample(w, k++);
+  if (k <= k1 && (k & 1)) o += sample(v, r, k++);
   for (; k < k1; k += 2) {
-    e += sample(w, k);
-    o += sample(w, k + 1);
+    e += sample(v, r, k);
+    o += sample(v, r, k + 1);
   }
-  if (k == k1) e += sample(w, k);
+  if (k == k1) e += sample(v, r, k);
 }
 
-// Ray sum (scaled by the plane step) of pixel (iv, iu) at angle theta. W
-// receives the plane step the transpose weights this ray with (0 for rays that
-// are not sampled), exactly as bp_weight_kernel computes it.
+// Ray sum (scaled by the plane step) of pixel (iv, iu) at angle theta. If W
+// is given it receives ray_weight. Values needed only after the plane loop
+// are computed after it, which keeps registers free for loads in flight.
 __device__ __forceinline__ float fp_ray_total(const AngleParams& ap,
                                               const ColumnEntry* __restrict__ columns,
                                               const float* __restrict__ ws,
                                               const DeviceGeometry& g, int iv, int iu, int theta,
-                                              float& W) {
-  const RayWalk w = prepare_ray(ap, columns, ws, g, iv, iu, theta);
-  W = w.W;
+                                              float* W) {
+  const RaySpan s = prepare_span(ap, columns, g, iv, iu, theta);
   float e = 0.0f, o = 0.0f;
-  walk(w, w.k0, w.k1, e, o);
-  return w.k0 <= w.k1 ? (e + o) * w.W : 0.0f;
+  walk(copy_view(ap, ws), s.r, s.k0, s.k1, e, o);
+  if (W) *W = ray_weight(ap, s.r);
+  return s.k0 <= s.k1 ? (e + o) * ray_step(ap, s.r) : 0.0f;
 }
 
 // Two adjacent angles of one pixel. When both use the same volume copy their
-// planes are walked together, so the second ray's taps (near the first's)
-// hit lines the first just brought into L1. Results equal fp_ray_total's.
+// planes are walked together through one base pointer and one set of strides,
+// so the second ray's taps (near the first's) hit lines the first just
+// brought into L1. Results equal fp_ray_total's.
 __device__ __forceinline__ void fp_ray_pair(const AngleParams& apa, const AngleParams& apb,
                                             const ColumnEntry* __restrict__ columns,
                                             const float* __restrict__ ws,
                                             const DeviceGeometry& g, int iv, int iu, int theta,
-                                            float& ta, float& tb) {
-  const RayWalk a = prepare_ray(apa, columns, ws, g, iv, iu, theta);
-  const RayWalk b = prepare_ray(apb, columns, ws, g, iv, iu, theta + 1);
+                                            float& ta, float& tb, float* Wa, float* Wb) {
+  const RaySpan a = prepare_span(apa, columns, g, iv, iu, theta);
+  const RaySpan b = prepare_span(apb, columns, g, iv, iu, theta + 1);
+  const CopyView va = copy_view(apa, ws);
   float ea = 0.0f, oa = 0.0f, eb = 0.0f, ob = 0.0f;
   const int lo = max(a.k0, b.k0), hi = min(a.k1, b.k1);
   if (apa.layout == apb.layout && lo <= hi) {
-    walk(a, a.k0, lo - 1, ea, oa);
-    walk(b, b.k0, lo - 1, eb, ob);
+    walk(va, a.r, a.k0, lo - 1, ea, oa);
+    walk(va, b.r, b.k0, lo - 1, eb, ob);
     int k = lo;
     if (k & 1) {
-      oa += sample(a, k);
-      ob += sample(b, k);
+      oa += sample(va, a.r, k);
+      ob += sample(va, b.r, k);
       ++k;
     }
     for (; k < hi; k += 2) {
-      ea += sample(a, k);
-      eb += sample(b, k);
-      oa += sample(a, k + 1);
-      ob += sample(b, k + 1);
+      ea += sample(va, a.r, k);
+      eb += sample(va, b.r, k);
+      oa += sample(va, a.r, k + 1);
+      ob += sample(va, b.r, k + 1);
     }
     if (k == hi) {
-      ea += sample(a, k);
-      eb += sample(b, k);
+      ea += sample(va, a.r, k);
+      eb += sample(va, b.r, k);
     }
-    walk(a, hi + 1, a.k1, ea, oa);
-    walk(b, hi + 1, b.k1, eb, ob);
+    walk(va, a.r, hi + 1, a.k1, ea, oa);
+    walk(va, b.r, hi + 1, b.k1, eb, ob);
   } else {
-    walk(a, a.k0, a.k1, ea, oa);
-    walk(b, b.k0, b.k1, eb, ob);
+    walk(va, a.r, a.k0, a.k1, ea, oa);
+    walk(copy_view(apb, ws), b.r, b.k0, b.k1, eb, ob);
   }
-  ta = a.k0 <= a.k1 ? (ea + oa) * a.W : 0.0f;
-  tb = b.k0 <= b.k1 ? (eb + ob) * b.W : 0.0f;
+  ta = a.k0 <= a.k1 ? (ea + oa) * ray_step(apa, a.r) : 0.0f;
+  tb = b.k0 <= b.k1 ? (eb + ob) * ray_step(apb, b.r) : 0.0f;
+  if (Wa) *Wa = ray_weight(apa, a.r);
+  if (Wb) *Wb = ray_weight(apb, b.r);
 }
 
-// One thread per pixel and pair of adjacent angles (blockIdx.z = pair).
-__global__ void __launch_bounds__(kFpRows* kFpCols)
+// One thread per pixel and pair of adjacent angles; the linear block index
+// is mapped to a tile by the projector's schedule. The output offset and the
+// pair flag wait in shared memory during the walk (volatile, so they are not
+// kept in registers across it). Four resident blocks per SM leave 64
+// registers a thread, which the plane loop spends on loads in flight.
+__global__ void __launch_bounds__(kFpRows* kFpCols, 4)
     fp_ray_kernel(const AngleParams* __restrict__ params, const ColumnEntry* __restrict__ columns,
                   const float* __restrict__ ws, float* __restrict__ sino, DeviceGeometry g,
-                  int angle0, int additive) {
-  const int iv = blockIdx.x * kFpRows + threadIdx.x;
-  const int iu = blockIdx.y * kFpCols + threadIdx.y;
-  const int theta = angle0 + 2 * blockIdx.z;
+                  FpSchedule sched, int angle0, int additive) {
+  __shared__ volatile long long out_slot[kFpRows * kFpCols];
+  int rb, cb, pr;
+  fp_schedule_tile(sched, blockIdx.x, rb, cb, pr);
+  const int iv = rb * kFpRows + threadIdx.x;
+  const int iu = cb * kFpCols + threadIdx.y;
+  const int theta = angle0 + 2 * pr;
   if (iu >= g.cols || iv >= g.rows) return;
-  float ta, tb = 0.0f, W;
-  const bool pair = theta + 1 < g.nangles;
-  if (pair)
-    fp_ray_pair(params[theta], params[theta + 1], columns, ws, g, iv, iu, theta, ta, tb);
+  const int slot = threadIdx.y * kFpRows + threadIdx.x;
+  const bool pair_in = theta + 1 < g.nangles;
+  out_slot[slot] = (((long long)iv * g.nangles + theta) * g.cols + iu) * 2 + (pair_in ? 1 : 0);
+  float ta, tb = 0.0f;
+  if (pair_in)
+    fp_ray_pair(params[theta], params[theta + 1], columns, ws, g, iv, iu, theta, ta, tb,
+                nullptr, nullptr);
   else
-    ta = fp_ray_total(params[theta], columns, ws, g, iv, iu, theta, W);
-  float* out = sino + ((size_t)iv * g.nangles + theta) * g.cols + iu;
+    ta = fp_ray_total(params[theta], columns, ws, g, iv, iu, theta, nullptr);
+  const long long packed = out_slot[slot];
+  const bool pair = (packed & 1) != 0;
+  float* out = sino + (packed >> 1);
   if (additive) {
     out[0] += ta;
     if (pair) out[g.cols] += tb;
@@ -213,30 +247,45 @@ __global__ void __launch_bounds__(kFpRows* kFpCols)
 }
 
 // ---------------------------------------------------------------- batched SIRT
-// One launch over all jobs' (row block, column block, angle) tiles. Epilogue:
-// residual = W * (R * (y - A x)), which is what the plain recipe computes with
-// separate operations (y - A(x), times R, then the backprojector's W pass).
-__global__ void __launch_bounds__(kFpRows* kFpCols)
+// One launch over all jobs' (row block, column block, angle pair) tiles, the
+// angles paired as in fp_ray_kernel. Epilogue: residual = W * (R * (y - A x)),
+// which is what the plain recipe computes with separate operations (y - A(x),
+// times R, then the backprojector's W pass).
+__device__ __forceinline__ void sirt_residual(const SirtJobDev& job, size_t idx, float total,
+                                              float W) {
+  const float r = __fmul_rn(__fsub_rn(__ldg(job.y + idx), total), __ldg(job.R + idx));
+  // res has kRowPad zero rows above and below the detector (never written)
+  job.res[idx + (size_t)kRowPad * job.g.nangles * job.g.cols] = __fmul_rn(W, r);
+}
+
+__global__ void __launch_bounds__(kFpRows* kFpCols, 4)
     fp_sirt_batch_kernel(const SirtJobDev* __restrict__ jobs,
                          const long long* __restrict__ prefix, int n_jobs) {
+  __shared__ volatile long long idx_slot[kFpRows * kFpCols];
   const long long b = blockIdx.x;
   const int j = find_job(prefix, n_jobs, b);
   const SirtJobDev& job = jobs[j];
   const DeviceGeometry& g = job.g;
-  long long local = b - prefix[j];
-  const int rb = int(local % job.fp_row_blocks);
-  local /= job.fp_row_blocks;
-  const int cb = int(local % job.fp_col_blocks);
-  const int theta = int(local / job.fp_col_blocks);
+  int rb, cb, pair;
+  fp_schedule_tile(job.fp_sched, b - prefix[j], rb, cb, pair);
+  const int theta = 2 * pair;
   const int iv = rb * kFpRows + threadIdx.x;
   const int iu = cb * kFpCols + threadIdx.y;
   if (iu >= g.cols || iv >= g.rows) return;
-  float W;
-  const float total = fp_ray_total(job.params[theta], job.columns, job.fp_ws, g, iv, iu, theta, W);
-  const size_t idx = ((size_t)iv * g.nangles + theta) * g.cols + iu;
-  const float r = __fmul_rn(__fsub_rn(__ldg(job.y + idx), total), __ldg(job.R + idx));
-  // res has kRowPad zero rows above and below the detector (never written)
-  job.res[idx + (size_t)kRowPad * g.nangles * g.cols] = __fmul_rn(W, r);
+  const int slot = threadIdx.y * kFpRows + threadIdx.x;
+  const bool pair_in = theta + 1 < g.nangles;
+  idx_slot[slot] = (((long long)iv * g.nangles + theta) * g.cols + iu) * 2 + (pair_in ? 1 : 0);
+  float ta, tb = 0.0f, Wa, Wb = 0.0f;
+  if (pair_in)
+    fp_ray_pair(job.params[theta], job.params[theta + 1], job.columns, job.fp_ws, g, iv, iu,
+                theta, ta, tb, &Wa, &Wb);
+  else
+    ta = fp_ray_total(job.params[theta], job.columns, job.fp_ws, g, iv, iu, theta, &Wa);
+  const long long packed = idx_slot[slot];
+  const SirtJobDev& jb = jobs[j];
+  const size_t idx = size_t(packed >> 1);
+  sirt_residual(jb, idx, ta, Wa);
+  if (packed & 1) sirt_residual(jb, idx + jb.g.cols, tb, Wb);
 }
 
 // Layout copies of all jobs: blockIdx.y selects the (job, permutation) segment.
@@ -273,14 +322,48 @@ int launch_fp(const tsgb_projector* p, const float* vol, float* sino, bool addit
     fp_layout_kernel<<<grid, threads, 0, stream>>>(vol, workspace, lt.l[i], vstride[L.d],
                                                   vstride[L.a], vstride[L.b]);
   }
-  const dim3 block(kFpRows, kFpCols);
-  for (int a0 = 0; a0 < g.nangles; a0 += 2 * 65535) {
-    const int n = g.nangles - a0 < 2 * 65535 ? g.nangles - a0 : 2 * 65535;
-    const dim3 grid((g.rows + kFpRows - 1) / kFpRows, (g.cols + kFpCols - 1) / kFpCols, (n + 1) / 2);
-    fp_ray_kernel<<<grid, block, 0, stream>>>(p->d_params, p->d_columns, workspace, sino, g, a0,
-                                              additive ? 1 : 0);
+  const long long per_pair = (long long)((g.rows + kFpRows - 1) / kFpRows) *
+                             ((g.cols + kFpCols - 1) / kFpCols);
+  const long long chunk = fp_angle_chunk(g);
+  for (long long a0 = 0; a0 < g.nangles; a0 += chunk) {
+    const int n = int(g.nangles - a0 < chunk ? g.nangles - a0 : chunk);
+    const FpSchedule s = fp_schedule(p, (n + 1) / 2);
+    const long long blocks = per_pair * s.pairs;
+    fp_ray_kernel<<<unsigned(blocks), dim3(kFpRows, kFpCols), 0, stream>>>(
+        p->d_params, p->d_columns, workspace, sino, g, s, int(a0), additive ? 1 : 0);
   }
   return int(cudaGetLastError());
+}
+
+long long fp_angle_chunk(const DeviceGeometry& g) {
+  // Angle chunks keep the forward projector's 1-D grid below 2^31 blocks.
+  const long long per_pair = (long long)((g.rows + kFpRows - 1) / kFpRows) *
+                             ((g.cols + kFpCols - 1) / kFpCols);
+  const long long max_pairs = ((1LL << 31) - 1) / per_pair;
+  return 2 * (max_pairs < (1LL << 29) ? max_pairs : (1LL << 29));
+}
+
+FpSchedule fp_schedule(const tsgb_projector* p, int pairs) {
+  FpSchedule s;
+  s.row_blocks = (p->g.rows + kFpRows - 1) / kFpRows;
+  s.col_blocks = (p->g.cols + kFpCols - 1) / kFpCols;
+  s.pairs = pairs;
+  s.patch_rows = std::min(std::max(p->tuning.fp_patch_rows, 1), s.row_blocks);
+  s.patch_cols = std::min(std::max(p->tuning.fp_patch_cols, 1), s.col_blocks);
+  s.group_pairs = std::min(std::max(p->tuning.fp_group_pairs, 1), std::max(pairs, 1));
+  return s;
+}
+
+tsgb_tuning default_tuning(const DeviceGeometry&) {
+  tsgb_tuning t{};
+  // Patches of 256 detector rows x 32 columns and groups of 64 angles: the
+  // volume slab such a group crosses stays in L2 while it runs (fastest on a
+  // 512^3 cone scan with a 512 x 768 detector and 1024 angles, and within
+  // 3 % of the fastest at 256^3 / 360 angles).
+  t.fp_patch_rows = 256 / kFpRows;
+  t.fp_patch_cols = 32 / kFpCols;
+  t.fp_group_pairs = 32;
+  return t;
 }
 
 int launch_sirt_fp_batch(const SirtBatchDev& b, void* stream_) {

@@ -88,11 +88,20 @@ struct DeviceGeometry {
   int det_ss, vox_ss;       // supersampling factors
 };
 
+// Forward-projection tile order over one chunk of angles (tsgb_tuning):
+// groups of group_pairs angle pairs, each run over the detector patch by
+// patch (patch_rows x patch_cols tiles), row tiles fastest inside a patch.
+struct FpSchedule {
+  int row_blocks, col_blocks, pairs;  // tiles along rows and columns; angle pairs
+  int patch_rows, patch_cols, group_pairs;
+};
+
 }  // namespace tsgb
 
 struct tsgb_projector {
   int device;
   tsgb::DeviceGeometry g;
+  tsgb_tuning tuning;
   std::vector<tsgb::AngleParams> host_params;
   std::vector<tsgb::Layout> layouts;
   int64_t fp_workspace_floats = 0;
@@ -118,6 +127,13 @@ std::string build_plan(const tsgb_volume_desc* vol, const tsgb_projection_desc* 
                        std::vector<ColumnEntry>* columns,
                        std::vector<int>* sep_angles, std::vector<int>* gen_angles,
                        std::vector<int>* bil_fast, std::vector<int>* bil_slow);
+
+// Schedule of `pairs` angle pairs under the projector's tuning (fp.cu).
+FpSchedule fp_schedule(const tsgb_projector* p, int pairs);
+// Angles per forward-projection launch (fp.cu).
+long long fp_angle_chunk(const DeviceGeometry& g);
+// Default tuning of a new projector (fp.cu).
+tsgb_tuning default_tuning(const DeviceGeometry& g);
 
 // Sets the calling thread's message returned by tsgb_last_error (capi.cu).
 void set_last_error(const std::string& msg);

@@ -98,6 +98,28 @@ class Projector:
                 "bp_workspace_bytes"]
         return dict(zip(keys, [int(v) for v in out]))
 
+    TUNING_KEYS = ("fp_patch_rows", "fp_patch_cols", "fp_group_pairs")
+
+    def get_tuning(self, device_index=None):
+        """Launch schedule of the forward projector (see tsgb_tuning)."""
+        lib = _native.load()
+        t = _native.Tuning()
+        _native.check(lib.tsgb_projector_get_tuning(self.handle(_device_index(device_index)),
+                                                    ctypes.byref(t)), "tsgb_projector_get_tuning")
+        return {k: int(getattr(t, k)) for k in self.TUNING_KEYS}
+
+    def set_tuning(self, device_index=None, **values):
+        """Change schedule values (keys of ``get_tuning``); results stay bit-identical."""
+        unknown = set(values) - set(self.TUNING_KEYS)
+        if unknown:
+            raise ValueError(f"unknown tuning keys {sorted(unknown)}")
+        idx = _device_index(device_index)
+        cur = self.get_tuning(idx)
+        cur.update({k: int(v) for k, v in values.items()})
+        t = _native.Tuning(**cur)
+        _native.check(_native.load().tsgb_projector_set_tuning(self.handle(idx), ctypes.byref(t)),
+                      "tsgb_projector_set_tuning")
+
     def __del__(self):
         handles, self._handles = getattr(self, "_handles", {}), {}
         if handles and _native._lib is not None:
@@ -106,6 +128,12 @@ class Projector:
                     _native._lib.tsgb_projector_destroy(h)
                 except Exception:
                     pass
+
+
+def _device_index(device_index):
+    if device_index is None:
+        return torch.cuda.current_device()
+    return int(device_index)
 
 
 def create_projector(volume_geometry, projection_geometry, *, voxel_supersampling=1,
