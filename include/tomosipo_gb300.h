@@ -112,9 +112,10 @@ int tsgb_direct_fp_noalloc(const tsgb_volume_desc* vol, const tsgb_projection_de
 
 /* One job of a batched SIRT solve: x += C * A^T(R * (y - A x)) per iteration.
  * All buffers are device memory on the projector's device: vol, C (volume
- * shaped), sino, R (sinogram shaped), residual (sinogram shaped plus two
- * rows above and two below the detector, i.e. (rows + 4) * angles * cols
- * floats, zeroed by the caller once), fp_workspace (tsgb_fp_workspace_bytes). The job's angles must all use the separable
+ * shaped), sino, R (sinogram shaped), residual (2 * (rows + 4) * angles * cols
+ * floats, zeroed by the caller once: the backprojector's row-pair layout with
+ * two padding rows above and below the detector), fp_workspace
+ * (tsgb_fp_workspace_bytes). The job's angles must all use the separable
  * backprojector (det_v along z: circular and helical geometries). */
 typedef struct {
   tsgb_projector* projector;

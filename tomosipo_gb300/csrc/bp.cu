@@ -36,41 +36,58 @@ constexpr int kBpY = kBpTileY;      // warps along y
 constexpr int kRunZ = kBpRunZ;      // voxels along z per thread (matched)
 constexpr int kRunZBil = 8;         // voxels along z per thread (bilinear)
 
-__global__ void __launch_bounds__(256)
-    bp_weight_kernel(const AngleParams* __restrict__ params,
-                     const ColumnEntry* __restrict__ columns, const float* __restrict__ sino,
-                     float* __restrict__ out, DeviceGeometry g) {
-  const int iu = blockIdx.x * 32 + threadIdx.x;
-  const int iv = blockIdx.y * 8 + threadIdx.y;
-  const int theta = blockIdx.z;
-  if (iu >= g.cols || iv >= g.rows) return;
-  const AngleParams& ap = params[theta];
+// W * y of pixel (iv, iu) at angle theta (0 for rows outside the detector and
+// for rays the forward projector does not sample).
+__device__ __forceinline__ float weighted_pixel(const AngleParams& ap,
+                                                const ColumnEntry* __restrict__ columns,
+                                                const float* __restrict__ sino,
+                                                const DeviceGeometry& g, int iv, int iu,
+                                                int theta) {
+  if (iv < 0 || iv >= g.rows) return 0.0f;
   const float vt = float(iv - g.ov);
   const Ray r = ap.separable ? ray_column(columns[(size_t)theta * g.cols + iu], vt)
                              : ray_general(ap, float(iu - g.ou), vt);
-  const size_t idx = ((size_t)iv * g.nangles + theta) * g.cols + iu;
   float w = 0.0f;
   if (finite_ray(r) && fabsf(r.ma) <= kMaxSlope && fabsf(r.mb) <= kMaxSlope) w = ray_step(ap, r);
-  // out has kRowPad zero rows above and below the detector
-  out[idx + (size_t)kRowPad * g.nangles * g.cols] = w * __ldg(sino + idx);
+  return w * __ldg(sino + ((size_t)iv * g.nangles + theta) * g.cols + iu);
+}
+
+// Row-pair weighted sinogram: element (iv, theta, iu) holds (W y[iv], W y[iv+1])
+// for iv = -1 .. rows-1 (blockIdx.y / threadIdx.y count from iv = -1), so one
+// 8-byte load gives the backprojector both rows of a tap. Elements iv = -2,
+// rows and rows+1 (the padding) are zeroed by the caller. `out` points at
+// element (0, 0, 0); rows are nangles * cols elements apart.
+__global__ void __launch_bounds__(256)
+    bp_weight_kernel(const AngleParams* __restrict__ params,
+                     const ColumnEntry* __restrict__ columns, const float* __restrict__ sino,
+                     float2* __restrict__ out, DeviceGeometry g) {
+  const int iu = blockIdx.x * 32 + threadIdx.x;
+  const int iv = blockIdx.y * 8 + threadIdx.y - 1;
+  const int theta = blockIdx.z;
+  if (iu >= g.cols || iv >= g.rows) return;
+  const AngleParams& ap = params[theta];
+  const float a = weighted_pixel(ap, columns, sino, g, iv, iu, theta);
+  const float b = weighted_pixel(ap, columns, sino, g, iv + 1, iu, theta);
+  out[((long long)iv * g.nangles + theta) * g.cols + iu] = make_float2(a, b);
 }
 
 // Matched backprojection of the angles in `angles` for the voxel column
 // (x, y) and the kRun voxels z0 .. z0 + kRun - 1, accumulated into acc.
-// sinow is the W-weighted sinogram with kRowPad zero rows above and below the
-// detector (rows -kRowPad .. rows + kRowPad - 1), so the two-row path reads
-// without bounds tests once its row index is clamped into the padding.
-// Offsets are 32-bit unless kWide (padded sinogram of 2^31 floats or more).
+// sinow is the row-pair weighted sinogram (bp_weight_kernel) with kRowPad
+// padding rows above and below the detector (rows -kRowPad .. rows + kRowPad
+// - 1), so the two-row path reads both rows with one load and without bounds
+// tests once its row index is clamped into the padding. Offsets (in pairs)
+// are 32-bit unless kWide (padded sinogram of 2^31 pairs or more).
 template <int kRun, bool kWide>
 __device__ __forceinline__ void bp_separable_accumulate(
     const AngleParams* __restrict__ params, const ColumnEntry* __restrict__ columns,
-    const int* __restrict__ angles, int n_angles, const float* __restrict__ sinow,
+    const int* __restrict__ angles, int n_angles, const float2* __restrict__ sinow,
     const DeviceGeometry& g, int x, int y, int z0, float (&acc)[kRun]) {
   using Offset = typename std::conditional<kWide, long long, int>::type;
   const float xt = float(x - g.ox), yt = float(y - g.oy);
   const float zt0 = float(z0 - g.oz);
   const Offset rs = Offset(g.nangles) * g.cols;  // row stride
-  const float* __restrict__ sinow0 = sinow + (long long)kRowPad * rs;  // row 0
+  const float2* __restrict__ sinow0 = sinow + (long long)kRowPad * rs;  // row 0
   const float vmin = float(-kRowPad - g.ov), vmax = float(g.rows - g.ov);
   const float4* __restrict__ col4 = reinterpret_cast<const float4*>(columns);
 #pragma unroll
@@ -92,7 +109,7 @@ __device__ __forceinline__ void bp_separable_accumulate(
     const float u2 = __fdividef(fmaf(th, ap.e[0], -A0), fmaf(-th, ap.e[1], A1));
     const int iu_lo = max(0, (int)floorf(clamp_coord(fminf(u1, u2))) + 1 + g.ou);
     const int iu_hi = min(g.cols - 1, (int)ceilf(clamp_coord(fmaxf(u1, u2))) - 1 + g.ou);
-    const float* __restrict__ sino_theta = sinow0 + (size_t)theta * g.cols;
+    const float2* __restrict__ sino_theta = sinow0 + (size_t)theta * g.cols;
     for (int iu = iu_lo; iu <= iu_hi; ++iu) {
       const size_t ci = ((size_t)theta * g.cols + iu) * 2;
       const float4 c0 = __ldg(col4 + ci);      // Xa, ma, P, Q
@@ -103,7 +120,7 @@ __device__ __forceinline__ void bp_separable_accumulate(
       const float B = fmaf(kt, c0.w, c0.z);
       const float Sl = fmaf(kt, c1.y, c1.x);
       const float inv = __fdividef(1.0f, Sl);
-      const float* __restrict__ col = sino_theta + iu;
+      const float2* __restrict__ col = sino_theta + iu;
       if (fabsf(Sl) >= 1.0f) {
         // Tent half-width 1/|Sl| <= 1 row: only rows floor(v*) and floor(v*)+1.
         const float vs0 = (zt0 - B) * inv;
@@ -114,10 +131,9 @@ __device__ __forceinline__ void bp_separable_accumulate(
           // both reads inside the padding (NaN clamps to the low end).
           const float v0 = fminf(fmaxf(floorf(vs), vmin), vmax);
           const float Bj = B - (zt0 + float(j));
-          const float w0 = tent(fmaf(v0, Sl, Bj));
-          const float w1 = tent(fmaf(v0 + 1.0f, Sl, Bj));
-          const float* p = col + Offset((int)v0 + g.ov) * rs;
-          acc[j] = fmaf(h, fmaf(w0, __ldg(p), w1 * __ldg(p + rs)), acc[j]);
+          const float t0 = fmaf(v0, Sl, Bj);  // q_b - z of row v0's ray
+          const float2 yy = __ldg(col + Offset((int)v0 + g.ov) * rs);
+          acc[j] = fmaf(h, fmaf(tent(t0), yy.x, tent(t0 + Sl) * yy.y), acc[j]);
         }
       } else {
 #pragma unroll
@@ -129,7 +145,7 @@ __device__ __forceinline__ void bp_separable_accumulate(
           float s = 0.0f;
           for (int iv = iv_lo; iv <= iv_hi; ++iv) {
             const float w = tent(fmaf(float(iv - g.ov), Sl, Bj));
-            s = fmaf(w, __ldg(col + Offset(iv) * rs), s);
+            s = fmaf(w, __ldg(col + Offset(iv) * rs).x, s);
           }
           acc[j] = fmaf(h, s, acc[j]);
         }
@@ -143,7 +159,7 @@ template <int kRun, bool kWide>
 __global__ void __launch_bounds__(kBpX* kBpY)
     bp_separable_kernel(const AngleParams* __restrict__ params,
                         const ColumnEntry* __restrict__ columns, const int* __restrict__ angles,
-                        int n_angles, const float* __restrict__ sinow, float* __restrict__ vol,
+                        int n_angles, const float2* __restrict__ sinow, float* __restrict__ vol,
                         DeviceGeometry g, int additive) {
   const int x = blockIdx.x * kBpX + threadIdx.x;
   const int y = blockIdx.y * kBpY + threadIdx.y;
@@ -189,7 +205,8 @@ __global__ void __launch_bounds__(kBpX* kBpY, 9)
   float acc[kRun];
   // batch creation rejects jobs whose padded sinogram needs 64-bit offsets
   bp_separable_accumulate<kRun, false>(job.params, job.columns, job.sep_angles, job.n_sep,
-                                       job.res, g, x, y, z0, acc);
+                                       reinterpret_cast<const float2*>(job.res), g, x, y, z0,
+                                       acc);
 #pragma unroll
   for (int j = 0; j < kRun; ++j) {
     const int z = z0 + j;
@@ -208,7 +225,7 @@ __device__ __forceinline__ float coord(int axis, float z, float y, float x) {
 __global__ void __launch_bounds__(128)
     bp_general_kernel(const AngleParams* __restrict__ params,
                       const ColumnEntry* __restrict__ columns, const int* __restrict__ angles,
-                      int n_angles, const float* __restrict__ sinow, float* __restrict__ vol,
+                      int n_angles, const float2* __restrict__ sinow, float* __restrict__ vol,
                       DeviceGeometry g, int additive) {
   const int x = blockIdx.x * 32 + threadIdx.x;
   const int y = blockIdx.y * 4 + threadIdx.y;
@@ -247,7 +264,7 @@ __global__ void __launch_bounds__(128)
     const int iu_hi = min(g.cols - 1, (int)ceilf(clamp_coord(umax)) - 1 + g.ou);
     const int iv_lo = max(0, (int)floorf(clamp_coord(vmin)) + 1 + g.ov);
     const int iv_hi = min(g.rows - 1, (int)ceilf(clamp_coord(vmax)) - 1 + g.ov);
-    const float* base = sinow + ((size_t)kRowPad * g.nangles + theta) * g.cols;
+    const float2* base = sinow + ((size_t)kRowPad * g.nangles + theta) * g.cols;
     for (int iv = iv_lo; iv <= iv_hi; ++iv) {
       const float vt = float(iv - g.ov);
       for (int iu = iu_lo; iu <= iu_hi; ++iu) {
@@ -256,7 +273,7 @@ __global__ void __launch_bounds__(128)
         const float wa = tent(fmaf(kt, r.ma, r.Xa) - it);
         const float wb = tent(fmaf(kt, r.mb, r.Xb) - jt);
         const float w = wa * wb;
-        if (w > 0.0f) acc = fmaf(w, __ldg(base + (size_t)iv * row_stride + iu), acc);
+        if (w > 0.0f) acc = fmaf(w, __ldg(base + (size_t)iv * row_stride + iu).x, acc);
       }
     }
   }
@@ -453,23 +470,23 @@ int launch_bp_matched(const tsgb_projector* p, float* vol, const float* sino, bo
                       float* workspace, void* stream_) {
   cudaStream_t stream = static_cast<cudaStream_t>(stream_);
   const DeviceGeometry& g = p->g;
+  float2* pairs = reinterpret_cast<float2*>(workspace);
+  const size_t rs = (size_t)g.nangles * g.cols;  // elements between rows
   {
     const dim3 block(32, 8);
     for (int a0 = 0; a0 < g.nangles; a0 += 65535) {
       const int n = g.nangles - a0 < 65535 ? g.nangles - a0 : 65535;
-      const dim3 grid((g.cols + 31) / 32, (g.rows + 7) / 8, n);
+      const dim3 grid((g.cols + 31) / 32, (g.rows + 1 + 7) / 8, n);
       // offset the angle through the pointers: rows are strided by nangles*cols
       bp_weight_kernel<<<grid, block, 0, stream>>>(p->d_params + a0, p->d_columns + (size_t)a0 * g.cols,
                                                    sino + (size_t)a0 * g.cols,
-                                                   workspace + (size_t)a0 * g.cols, g);
+                                                   pairs + kRowPad * rs + (size_t)a0 * g.cols, g);
     }
   }
-  {
-    // zero the kRowPad rows above and below the detector
-    const size_t pad = (size_t)kRowPad * g.nangles * g.cols * sizeof(float);
-    cudaMemsetAsync(workspace, 0, pad, stream);
-    cudaMemsetAsync(workspace + (size_t)(kRowPad + g.rows) * g.nangles * g.cols, 0, pad, stream);
-  }
+  // zero the padding rows the weight pass does not write: -kRowPad .. -2 and
+  // rows .. rows + kRowPad - 1
+  cudaMemsetAsync(pairs, 0, (kRowPad - 1) * rs * sizeof(float2), stream);
+  cudaMemsetAsync(pairs + (kRowPad + g.rows) * rs, 0, kRowPad * rs * sizeof(float2), stream);
   bool written = false;
   if (p->n_separable_bp > 0) {
     const dim3 block(kBpX, kBpY);
@@ -477,11 +494,11 @@ int launch_bp_matched(const tsgb_projector* p, float* vol, const float* sino, bo
     const bool wide = (size_t)(g.rows + 2 * kRowPad) * g.nangles * g.cols >= (size_t(1) << 31);
     if (wide)
       bp_separable_kernel<kRunZ, true><<<grid, block, 0, stream>>>(
-          p->d_params, p->d_columns, p->d_sep_angles, p->n_separable_bp, workspace, vol, g,
+          p->d_params, p->d_columns, p->d_sep_angles, p->n_separable_bp, pairs, vol, g,
           additive ? 1 : 0);
     else
       bp_separable_kernel<kRunZ, false><<<grid, block, 0, stream>>>(
-          p->d_params, p->d_columns, p->d_sep_angles, p->n_separable_bp, workspace, vol, g,
+          p->d_params, p->d_columns, p->d_sep_angles, p->n_separable_bp, pairs, vol, g,
           additive ? 1 : 0);
     written = true;
   }
@@ -489,7 +506,7 @@ int launch_bp_matched(const tsgb_projector* p, float* vol, const float* sino, bo
     const dim3 block(32, 4);
     const dim3 grid((g.nx + 31) / 32, (g.ny + 3) / 4, g.nz);
     bp_general_kernel<<<grid, block, 0, stream>>>(p->d_params, p->d_columns, p->d_gen_angles,
-                                                  p->n_general_bp, workspace, vol, g,
+                                                  p->n_general_bp, pairs, vol, g,
                                                   (additive || written) ? 1 : 0);
   }
   return int(cudaGetLastError());

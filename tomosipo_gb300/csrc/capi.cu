@@ -132,7 +132,8 @@ int64_t tsgb_bp_workspace_bytes(const tsgb_projector* p, int32_t bp_kind) {
                                    (p->g.cols + 2 * tsgb::kColPad) * int64_t(sizeof(float))
                              : 0;
   if (bp_kind != TSGB_BP_MATCHED) return fail(TSGB_ERR_INVALID, "unknown bp_kind");
-  return int64_t(p->g.rows + 2 * tsgb::kRowPad) * p->g.nangles * p->g.cols * int64_t(sizeof(float));
+  // row-pair weighted sinogram: two floats per pixel, kRowPad padding rows
+  return int64_t(p->g.rows + 2 * tsgb::kRowPad) * p->g.nangles * p->g.cols * int64_t(2 * sizeof(float));
 }
 
 int tsgb_projector_shapes(const tsgb_projector* p, int64_t vol_shape[3], int64_t sino_shape[3]) {

@@ -254,8 +254,15 @@ __global__ void __launch_bounds__(kFpRows* kFpCols, 4)
 __device__ __forceinline__ void sirt_residual(const SirtJobDev& job, size_t idx, float total,
                                               float W) {
   const float r = __fmul_rn(__fsub_rn(__ldg(job.y + idx), total), __ldg(job.R + idx));
-  // res has kRowPad zero rows above and below the detector (never written)
-  job.res[idx + (size_t)kRowPad * job.g.nangles * job.g.cols] = __fmul_rn(W, r);
+  const float v = __fmul_rn(W, r);
+  // res is the backprojector's row-pair sinogram (kRowPad padding rows above
+  // and below the detector, zeroed once by the caller and never written):
+  // this pixel is the first value of its own row's pair and the second of
+  // the pair one row up.
+  const size_t rs = (size_t)job.g.nangles * job.g.cols;
+  float* e = job.res + 2 * (idx + kRowPad * rs);
+  e[0] = v;
+  e[1 - 2 * (long long)rs] = v;
 }
 
 __global__ void __launch_bounds__(kFpRows* kFpCols, 4)

@@ -68,8 +68,9 @@ class SirtJobState:
             self.x = (torch.zeros(A.domain_shape, device=device) if x_init is None
                       else x_init.to(device, torch.float32).contiguous().clone())
             rows, angles, cols = A.range_shape
-            # two zero detector rows above and below (read as padding by the BP)
-            self.res = torch.zeros((rows + 4) * angles * cols, device=device)
+            # the backprojector's row-pair layout (two floats per pixel) with two
+            # zero detector rows above and below, read as padding
+            self.res = torch.zeros(2 * (rows + 4) * angles * cols, device=device)
             nbytes = A.projector.workspace_bytes(device.index, True)
             self.ws = torch.empty(max(nbytes, 4) // 4, device=device)
 
@@ -80,7 +81,7 @@ class SirtJobState:
         rows, angles, cols = A.range_shape
         sino = 4 * rows * angles * cols
         stats_ws = A.projector.stats(torch.cuda.current_device())["fp_workspace_bytes"]
-        return 2 * vol + 3 * sino + 16 * angles * cols + stats_ws
+        return 2 * vol + 4 * sino + 32 * angles * cols + stats_ws
 
 
 class NativeBatch:
