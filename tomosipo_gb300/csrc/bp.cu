@@ -123,17 +123,36 @@ __device__ __forceinline__ void bp_separable_accumulate(
       const float2* __restrict__ col = sino_theta + iu;
       if (fabsf(Sl) >= 1.0f) {
         // Tent half-width 1/|Sl| <= 1 row: only rows floor(v*) and floor(v*)+1.
+        // Voxel j's row position vs = (z_j - B) / Sl; row v0's ray passes the
+        // plane at q_b - z_j = v0 Sl + (B - zt0) - j. The column weight h is
+        // folded into the tents: h tent(t) = max(0, h - h |t|).
         const float vs0 = (zt0 - B) * inv;
+        const float vs1 = fmaf(float(kRun - 1), inv, vs0);
+        const float C0 = B - zt0;
+        const float nh = -h;
+        const float2* __restrict__ colv = col + Offset(g.ov) * rs;  // row 0 of this column
+        // vs is monotone in j: if both ends select rows inside [vmin, vmax]
+        // every voxel does, and no clamping is needed (NaN fails the test).
+        if (fminf(vs0, vs1) >= vmin && fmaxf(vs0, vs1) < vmax + 1.0f) {
 #pragma unroll
-        for (int j = 0; j < kRun; ++j) {
-          const float vs = fmaf(float(j), inv, vs0);
-          // Rows outside [-kRowPad, rows] hold zeros either way: clamping keeps
-          // both reads inside the padding (NaN clamps to the low end).
-          const float v0 = fminf(fmaxf(floorf(vs), vmin), vmax);
-          const float Bj = B - (zt0 + float(j));
-          const float t0 = fmaf(v0, Sl, Bj);  // q_b - z of row v0's ray
-          const float2 yy = __ldg(col + Offset((int)v0 + g.ov) * rs);
-          acc[j] = fmaf(h, fmaf(tent(t0), yy.x, tent(t0 + Sl) * yy.y), acc[j]);
+          for (int j = 0; j < kRun; ++j) {
+            const float v0 = floorf(fmaf(float(j), inv, vs0));
+            const float t0 = fmaf(v0, Sl, C0) - float(j);
+            const float2 yy = __ldg(colv + Offset((int)v0) * rs);
+            acc[j] = fmaf(fmaxf(0.0f, fmaf(nh, fabsf(t0), h)), yy.x,
+                          fmaf(fmaxf(0.0f, fmaf(nh, fabsf(t0 + Sl), h)), yy.y, acc[j]));
+          }
+        } else {
+#pragma unroll
+          for (int j = 0; j < kRun; ++j) {
+            // Rows outside [-kRowPad, rows] hold zeros either way: clamping
+            // keeps both reads inside the padding (NaN clamps to the low end).
+            const float v0 = fminf(fmaxf(floorf(fmaf(float(j), inv, vs0)), vmin), vmax);
+            const float t0 = fmaf(v0, Sl, C0) - float(j);
+            const float2 yy = __ldg(colv + Offset((int)v0) * rs);
+            acc[j] = fmaf(fmaxf(0.0f, fmaf(nh, fabsf(t0), h)), yy.x,
+                          fmaf(fmaxf(0.0f, fmaf(nh, fabsf(t0 + Sl), h)), yy.y, acc[j]));
+          }
         }
       } else {
 #pragma unroll
