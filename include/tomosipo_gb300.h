@@ -129,14 +129,18 @@ typedef struct {
 
 typedef struct tsgb_sirt_batch tsgb_sirt_batch;
 
-/* Build the device job tables of a batch (one small allocation). No
- * counterpart in the reference, whose SIRT is a Python loop per job
- * (README.md:150-163); results equal that loop's. */
+/* Build a batch: orders the jobs largest first and creates its streams (at
+ * most 8) and events on the current device. No counterpart in the reference,
+ * whose SIRT is a Python loop per job (README.md:150-163); results are bitwise
+ * equal to that loop's. */
 int tsgb_sirt_batch_create(const tsgb_sirt_job* jobs, int32_t n_jobs, tsgb_sirt_batch** out);
 
-/* Run ``iterations`` SIRT iterations of every job: three kernel launches per
- * iteration over all jobs, on ``stream``. Allocates nothing; capturable in a
- * CUDA graph. */
+/* Run ``iterations`` SIRT iterations of every job. Per job and iteration: its
+ * padded volume copies, the forward projection writing the residual and the
+ * backprojection applying the update, on the batch's streams, forked from and
+ * joined back into ``stream`` (jobs never wait for each other). Allocates
+ * nothing; capturable in a CUDA graph (the fork and join become its
+ * branches). */
 int tsgb_sirt_batch_iterate(tsgb_sirt_batch* b, int32_t iterations, void* stream);
 
 /* Free a batch's tables (not the jobs' buffers). */

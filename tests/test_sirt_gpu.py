@@ -72,14 +72,17 @@ def test_batched_equals_plain_and_alone_equals_mix(dev):
 
 
 def test_batched_graph_replay_equals_eager(dev):
-    jobs = [_job(dev, 32, True, 40, 5), _job(dev, 48, False, 70, 6)]
+    # more jobs than the batch's 8 streams, and 13 iterations as graphs of 5, 5 and 3
+    jobs = [_job(dev, 16 + 4 * (i % 4), i % 2 == 0, 12 + 3 * i, 20 + i) for i in range(11)]
     eager = BatchedSirt([(A, y) for A, y, _ in jobs])
-    eager.run(5, graph=False)
+    eager.run(13, graph=False)
     graphed = BatchedSirt([(A, y) for A, y, _ in jobs])
-    graphed.run(5, graph=True)
+    graphed.graph_iterations = 5
+    graphed.run(13, graph=True)
     torch.cuda.synchronize()
-    for a, b in zip(eager.x, graphed.x):
+    for (A, y, _), a, b in zip(jobs, eager.x, graphed.x):
         assert torch.equal(a, b)
+    assert torch.equal(eager.x[3], sirt(jobs[3][0], jobs[3][1], 13))
 
 
 def test_batched_rejects_tilted_detectors(dev):

@@ -174,12 +174,14 @@ __device__ __forceinline__ void bp_separable_accumulate(
 }
 
 // One thread per (x, y) voxel column and run of kRun voxels along z.
-template <int kRun, bool kWide>
+// kSirt: SIRT update x += C * A^T(res) instead of writing the backprojection,
+// rounded as the plain recipe's x += C * bp (C is then the per-voxel weight).
+template <int kRun, bool kWide, bool kSirt>
 __global__ void __launch_bounds__(kBpX* kBpY)
     bp_separable_kernel(const AngleParams* __restrict__ params,
                         const ColumnEntry* __restrict__ columns, const int* __restrict__ angles,
                         int n_angles, const float2* __restrict__ sinow, float* __restrict__ vol,
-                        DeviceGeometry g, int additive) {
+                        DeviceGeometry g, int additive, const float* __restrict__ C) {
   const int x = blockIdx.x * kBpX + threadIdx.x;
   const int y = blockIdx.y * kBpY + threadIdx.y;
   const int z0 = blockIdx.z * kRun;
@@ -190,48 +192,13 @@ __global__ void __launch_bounds__(kBpX* kBpY)
   for (int j = 0; j < kRun; ++j) {
     const int z = z0 + j;
     if (z < g.nz) {
-      float* out = vol + ((size_t)z * g.ny + y) * g.nx + x;
-      if (additive)
-        *out += acc[j];
-      else
-        *out = acc[j];
-    }
-  }
-}
-
-// Batched SIRT backprojection over all jobs' voxel tiles; epilogue
-// x += C * A^T(res), rounded as the plain recipe's x += C * bp. The job
-// descriptor lives in global memory rather than in the parameter bank, which
-// costs registers; 9 resident blocks per SM keep it at bp_separable_kernel's
-// 56 registers (no spills).
-template <int kRun>
-__global__ void __launch_bounds__(kBpX* kBpY, 9)
-    bp_sirt_batch_kernel(const SirtJobDev* __restrict__ jobs, const long long* __restrict__ prefix,
-                         int n_jobs) {
-  const long long b = blockIdx.x;
-  const int jn = find_job(prefix, n_jobs, b);
-  const SirtJobDev& job = jobs[jn];
-  const DeviceGeometry& g = job.g;
-  long long local = b - prefix[jn];
-  const int xb = int(local % job.bp_xb);
-  local /= job.bp_xb;
-  const int yb = int(local % job.bp_yb);
-  const int zb = int(local / job.bp_yb);
-  const int x = xb * kBpX + threadIdx.x;
-  const int y = yb * kBpY + threadIdx.y;
-  const int z0 = zb * kRun;
-  if (x >= g.nx || y >= g.ny) return;
-  float acc[kRun];
-  // batch creation rejects jobs whose padded sinogram needs 64-bit offsets
-  bp_separable_accumulate<kRun, false>(job.params, job.columns, job.sep_angles, job.n_sep,
-                                       reinterpret_cast<const float2*>(job.res), g, x, y, z0,
-                                       acc);
-#pragma unroll
-  for (int j = 0; j < kRun; ++j) {
-    const int z = z0 + j;
-    if (z < g.nz) {
       const size_t idx = ((size_t)z * g.ny + y) * g.nx + x;
-      job.vol[idx] = __fadd_rn(job.vol[idx], __fmul_rn(acc[j], __ldg(job.C + idx)));
+      if (kSirt)
+        vol[idx] = __fadd_rn(vol[idx], __fmul_rn(acc[j], __ldg(C + idx)));
+      else if (additive)
+        vol[idx] += acc[j];
+      else
+        vol[idx] = acc[j];
     }
   }
 }
@@ -512,13 +479,13 @@ int launch_bp_matched(const tsgb_projector* p, float* vol, const float* sino, bo
     const dim3 grid((g.nx + kBpX - 1) / kBpX, (g.ny + kBpY - 1) / kBpY, (g.nz + kRunZ - 1) / kRunZ);
     const bool wide = (size_t)(g.rows + 2 * kRowPad) * g.nangles * g.cols >= (size_t(1) << 31);
     if (wide)
-      bp_separable_kernel<kRunZ, true><<<grid, block, 0, stream>>>(
+      bp_separable_kernel<kRunZ, true, false><<<grid, block, 0, stream>>>(
           p->d_params, p->d_columns, p->d_sep_angles, p->n_separable_bp, pairs, vol, g,
-          additive ? 1 : 0);
+          additive ? 1 : 0, nullptr);
     else
-      bp_separable_kernel<kRunZ, false><<<grid, block, 0, stream>>>(
+      bp_separable_kernel<kRunZ, false, false><<<grid, block, 0, stream>>>(
           p->d_params, p->d_columns, p->d_sep_angles, p->n_separable_bp, pairs, vol, g,
-          additive ? 1 : 0);
+          additive ? 1 : 0, nullptr);
     written = true;
   }
   if (p->n_general_bp > 0 || !written) {
@@ -531,13 +498,24 @@ int launch_bp_matched(const tsgb_projector* p, float* vol, const float* sino, bo
   return int(cudaGetLastError());
 }
 
-int launch_sirt_bp_batch(const SirtBatchDev& b, void* stream_) {
+int launch_bp_sirt(const tsgb_projector* p, float* vol, const float* C, const float* res,
+                   void* stream_) {
   cudaStream_t stream = static_cast<cudaStream_t>(stream_);
-  if (b.bp_blocks > 0)
-    bp_sirt_batch_kernel<kRunZ><<<unsigned(b.bp_blocks), dim3(kBpX, kBpY), 0, stream>>>(
-        b.jobs, b.bp_prefix, b.n_jobs);
+  const DeviceGeometry& g = p->g;
+  if (p->n_separable_bp == 0) return int(cudaGetLastError());
+  const float2* pairs = reinterpret_cast<const float2*>(res);
+  const dim3 block(kBpX, kBpY);
+  const dim3 grid((g.nx + kBpX - 1) / kBpX, (g.ny + kBpY - 1) / kBpY, (g.nz + kRunZ - 1) / kRunZ);
+  const bool wide = (size_t)(g.rows + 2 * kRowPad) * g.nangles * g.cols >= (size_t(1) << 31);
+  if (wide)
+    bp_separable_kernel<kRunZ, true, true><<<grid, block, 0, stream>>>(
+        p->d_params, p->d_columns, p->d_sep_angles, p->n_separable_bp, pairs, vol, g, 0, C);
+  else
+    bp_separable_kernel<kRunZ, false, true><<<grid, block, 0, stream>>>(
+        p->d_params, p->d_columns, p->d_sep_angles, p->n_separable_bp, pairs, vol, g, 0, C);
   return int(cudaGetLastError());
 }
+
 
 int launch_bp_bilinear(const tsgb_projector* p, float* vol, const float* sino, bool additive,
                        float* workspace, void* stream_) {

@@ -83,43 +83,7 @@ __device__ __forceinline__ bool finite_ray(const Ray& r) {
   return isfinite(r.Xa) && isfinite(r.ma) && isfinite(r.Xb) && isfinite(r.mb);
 }
 
-// ------------------------------------------------------------ batched SIRT
-// One SIRT job of a batch, as the batched kernels see it.
-struct SirtJobDev {
-  const AngleParams* params;
-  const ColumnEntry* columns;
-  const int* sep_angles;
-  int n_sep;
-  int wide;  // sinogram has >= 2^31 floats (64-bit row offsets)
-  DeviceGeometry g;
-  float* vol;         // x, updated in place
-  const float* y;     // measured sinogram
-  const float* R;     // per-ray weights (sinogram-shaped)
-  const float* C;     // per-voxel weights (volume-shaped)
-  float* res;         // W * R * (y - A x) (sinogram-shaped)
-  const float* fp_ws; // padded volume copies
-  FpSchedule fp_sched; // forward tile order over all of the job's angles
-  int bp_xb, bp_yb, bp_zb;
-};
-
-// One (job, axis permutation) padded volume copy.
-struct LayoutSegDev {
-  const float* vol;
-  float* out;
-  long long n_d, n_a, n_b;
-  long long s_d, s_a, s_b;
-};
-
-// Device tables of a batch plus launch sizes (host-side struct).
-struct SirtBatchDev {
-  SirtJobDev* jobs;
-  long long* fp_prefix;  // n_jobs + 1 block offsets
-  long long* bp_prefix;
-  LayoutSegDev* segs;
-  int n_jobs, n_segs;
-  long long fp_blocks, bp_blocks, seg_grid_x;
-};
-
+// ------------------------------------------------------------ FP tile order
 // Tile (row block, column block, angle pair) of linear block b under s. The
 // blocks of a group of pairs come first, inside a group the patches strip by
 // strip, inside a patch the pairs and then the tiles with row blocks fastest.
@@ -146,19 +110,6 @@ __device__ __forceinline__ void fp_schedule_tile(const FpSchedule& s, long long 
   const int t = int(b - q * tiles);
   rb = pr * s.patch_rows + t % rsz;
   cb = pc * s.patch_cols + t / rsz;
-}
-
-// Job whose block range [prefix[j], prefix[j+1]) holds block b.
-__device__ __forceinline__ int find_job(const long long* __restrict__ prefix, int n, long long b) {
-  int lo = 0, hi = n - 1;
-  while (lo < hi) {
-    const int mid = (lo + hi + 1) >> 1;
-    if (__ldg(prefix + mid) <= b)
-      lo = mid;
-    else
-      hi = mid - 1;
-  }
-  return lo;
 }
 
 }  // namespace tsgb

@@ -209,15 +209,34 @@ __device__ __forceinline__ void fp_ray_pair(const AngleParams& apa, const AngleP
   if (Wb) *Wb = ray_weight(apb, b.r);
 }
 
+// SIRT epilogue: residual W * (R * (y - A x)) of pixel idx, written where the
+// backprojector reads it. s.res is the row-pair sinogram of bp_weight_kernel
+// (kRowPad padding rows above and below the detector, zeroed once by the
+// caller and never written): the pixel is the first value of its own row's
+// pair and the second of the pair one row up. The plain recipe computes the
+// same products with separate operations (y - A(x), times R, then the
+// backprojector's W pass), rounded the same way.
+__device__ __forceinline__ void sirt_residual(const FpSirt& s, const DeviceGeometry& g,
+                                              long long idx, float total, float W) {
+  const float r = __fmul_rn(__fsub_rn(__ldg(s.y + idx), total), __ldg(s.R + idx));
+  const float v = __fmul_rn(W, r);
+  const long long rs = (long long)g.nangles * g.cols;
+  float* e = s.res + 2 * (idx + kRowPad * rs);
+  e[0] = v;
+  e[1 - 2 * rs] = v;
+}
+
 // One thread per pixel and pair of adjacent angles; the linear block index
 // is mapped to a tile by the projector's schedule. The output offset and the
 // pair flag wait in shared memory during the walk (volatile, so they are not
 // kept in registers across it). Four resident blocks per SM leave 64
 // registers a thread, which the plane loop spends on loads in flight.
+// kSirt: write the SIRT residual (sirt_residual) instead of the sinogram.
+template <bool kSirt>
 __global__ void __launch_bounds__(kFpRows* kFpCols, 4)
     fp_ray_kernel(const AngleParams* __restrict__ params, const ColumnEntry* __restrict__ columns,
                   const float* __restrict__ ws, float* __restrict__ sino, DeviceGeometry g,
-                  FpSchedule sched, int angle0, int additive) {
+                  FpSchedule sched, int angle0, int additive, FpSirt sirt) {
   __shared__ volatile long long out_slot[kFpRows * kFpCols];
   int rb, cb, pr;
   fp_schedule_tile(sched, blockIdx.x, rb, cb, pr);
@@ -228,94 +247,34 @@ __global__ void __launch_bounds__(kFpRows* kFpCols, 4)
   const int slot = threadIdx.y * kFpRows + threadIdx.x;
   const bool pair_in = theta + 1 < g.nangles;
   out_slot[slot] = (((long long)iv * g.nangles + theta) * g.cols + iu) * 2 + (pair_in ? 1 : 0);
-  float ta, tb = 0.0f;
+  float ta, tb = 0.0f, Wa = 0.0f, Wb = 0.0f;
   if (pair_in)
     fp_ray_pair(params[theta], params[theta + 1], columns, ws, g, iv, iu, theta, ta, tb,
-                nullptr, nullptr);
+                kSirt ? &Wa : nullptr, kSirt ? &Wb : nullptr);
   else
-    ta = fp_ray_total(params[theta], columns, ws, g, iv, iu, theta, nullptr);
+    ta = fp_ray_total(params[theta], columns, ws, g, iv, iu, theta, kSirt ? &Wa : nullptr);
   const long long packed = out_slot[slot];
   const bool pair = (packed & 1) != 0;
-  float* out = sino + (packed >> 1);
-  if (additive) {
-    out[0] += ta;
-    if (pair) out[g.cols] += tb;
+  const long long idx = packed >> 1;
+  if (kSirt) {
+    sirt_residual(sirt, g, idx, ta, Wa);
+    if (pair) sirt_residual(sirt, g, idx + g.cols, tb, Wb);
   } else {
-    out[0] = ta;
-    if (pair) out[g.cols] = tb;
-  }
-}
-
-// ---------------------------------------------------------------- batched SIRT
-// One launch over all jobs' (row block, column block, angle pair) tiles, the
-// angles paired as in fp_ray_kernel. Epilogue: residual = W * (R * (y - A x)),
-// which is what the plain recipe computes with separate operations (y - A(x),
-// times R, then the backprojector's W pass).
-__device__ __forceinline__ void sirt_residual(const SirtJobDev& job, size_t idx, float total,
-                                              float W) {
-  const float r = __fmul_rn(__fsub_rn(__ldg(job.y + idx), total), __ldg(job.R + idx));
-  const float v = __fmul_rn(W, r);
-  // res is the backprojector's row-pair sinogram (kRowPad padding rows above
-  // and below the detector, zeroed once by the caller and never written):
-  // this pixel is the first value of its own row's pair and the second of
-  // the pair one row up.
-  const size_t rs = (size_t)job.g.nangles * job.g.cols;
-  float* e = job.res + 2 * (idx + kRowPad * rs);
-  e[0] = v;
-  e[1 - 2 * (long long)rs] = v;
-}
-
-__global__ void __launch_bounds__(kFpRows* kFpCols, 4)
-    fp_sirt_batch_kernel(const SirtJobDev* __restrict__ jobs,
-                         const long long* __restrict__ prefix, int n_jobs) {
-  __shared__ volatile long long idx_slot[kFpRows * kFpCols];
-  const long long b = blockIdx.x;
-  const int j = find_job(prefix, n_jobs, b);
-  const SirtJobDev& job = jobs[j];
-  const DeviceGeometry& g = job.g;
-  int rb, cb, pair;
-  fp_schedule_tile(job.fp_sched, b - prefix[j], rb, cb, pair);
-  const int theta = 2 * pair;
-  const int iv = rb * kFpRows + threadIdx.x;
-  const int iu = cb * kFpCols + threadIdx.y;
-  if (iu >= g.cols || iv >= g.rows) return;
-  const int slot = threadIdx.y * kFpRows + threadIdx.x;
-  const bool pair_in = theta + 1 < g.nangles;
-  idx_slot[slot] = (((long long)iv * g.nangles + theta) * g.cols + iu) * 2 + (pair_in ? 1 : 0);
-  float ta, tb = 0.0f, Wa, Wb = 0.0f;
-  if (pair_in)
-    fp_ray_pair(job.params[theta], job.params[theta + 1], job.columns, job.fp_ws, g, iv, iu,
-                theta, ta, tb, &Wa, &Wb);
-  else
-    ta = fp_ray_total(job.params[theta], job.columns, job.fp_ws, g, iv, iu, theta, &Wa);
-  const long long packed = idx_slot[slot];
-  const SirtJobDev& jb = jobs[j];
-  const size_t idx = size_t(packed >> 1);
-  sirt_residual(jb, idx, ta, Wa);
-  if (packed & 1) sirt_residual(jb, idx + jb.g.cols, tb, Wb);
-}
-
-// Layout copies of all jobs: blockIdx.y selects the (job, permutation) segment.
-__global__ void fp_layout_batch_kernel(const LayoutSegDev* __restrict__ segs) {
-  const LayoutSegDev& s = segs[blockIdx.y];
-  const long long n_ap = s.n_a + 2 * kPad, n_bp = s.n_b + 2 * kPad;
-  const long long total = (long long)s.n_d * n_ap * n_bp;
-  for (long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x; idx < total;
-       idx += (long long)gridDim.x * blockDim.x) {
-    const long long jp = idx % n_bp, rest = idx / n_bp;
-    const long long ip = rest % n_ap, k = rest / n_ap;
-    const long long i = ip - kPad, jj = jp - kPad;
-    float v = 0.0f;
-    if (i >= 0 && i < s.n_a && jj >= 0 && jj < s.n_b)
-      v = __ldg(s.vol + k * s.s_d + i * s.s_a + jj * s.s_b);
-    s.out[idx] = v;
+    float* out = sino + idx;
+    if (additive) {
+      out[0] += ta;
+      if (pair) out[g.cols] += tb;
+    } else {
+      out[0] = ta;
+      if (pair) out[g.cols] = tb;
+    }
   }
 }
 
 }  // namespace
 
 int launch_fp(const tsgb_projector* p, const float* vol, float* sino, bool additive,
-              float* workspace, void* stream_) {
+              float* workspace, void* stream_, const FpSirt* sirt) {
   cudaStream_t stream = static_cast<cudaStream_t>(stream_);
   const DeviceGeometry& g = p->g;
   const LayoutTable lt = make_layout_table(p);
@@ -336,8 +295,12 @@ int launch_fp(const tsgb_projector* p, const float* vol, float* sino, bool addit
     const int n = int(g.nangles - a0 < chunk ? g.nangles - a0 : chunk);
     const FpSchedule s = fp_schedule(p, (n + 1) / 2);
     const long long blocks = per_pair * s.pairs;
-    fp_ray_kernel<<<unsigned(blocks), dim3(kFpRows, kFpCols), 0, stream>>>(
-        p->d_params, p->d_columns, workspace, sino, g, s, int(a0), additive ? 1 : 0);
+    if (sirt)
+      fp_ray_kernel<true><<<unsigned(blocks), dim3(kFpRows, kFpCols), 0, stream>>>(
+          p->d_params, p->d_columns, workspace, sino, g, s, int(a0), 0, *sirt);
+    else
+      fp_ray_kernel<false><<<unsigned(blocks), dim3(kFpRows, kFpCols), 0, stream>>>(
+          p->d_params, p->d_columns, workspace, sino, g, s, int(a0), additive ? 1 : 0, FpSirt{});
   }
   return int(cudaGetLastError());
 }
@@ -373,16 +336,5 @@ tsgb_tuning default_tuning(const DeviceGeometry&) {
   return t;
 }
 
-int launch_sirt_fp_batch(const SirtBatchDev& b, void* stream_) {
-  cudaStream_t stream = static_cast<cudaStream_t>(stream_);
-  if (b.n_segs > 0) {
-    const dim3 grid(unsigned(b.seg_grid_x), unsigned(b.n_segs));
-    fp_layout_batch_kernel<<<grid, 256, 0, stream>>>(b.segs);
-  }
-  if (b.fp_blocks > 0)
-    fp_sirt_batch_kernel<<<unsigned(b.fp_blocks), dim3(kFpRows, kFpCols), 0, stream>>>(
-        b.jobs, b.fp_prefix, b.n_jobs);
-  return int(cudaGetLastError());
-}
 
 }  // namespace tsgb

@@ -138,18 +138,29 @@ tsgb_tuning default_tuning(const DeviceGeometry& g);
 // Sets the calling thread's message returned by tsgb_last_error (capi.cu).
 void set_last_error(const std::string& msg);
 
+// SIRT epilogue of the forward projection: instead of a sinogram it writes
+// res = W * (R * (y - A x)) in the backprojector's row-pair layout, where W is
+// each ray's plane step (see bp_weight_kernel). res holds
+// 2 * (rows + 2 kRowPad) * nangles * cols floats whose padding rows are zero.
+struct FpSirt {
+  const float* y;  // measured sinogram
+  const float* R;  // per-ray weights (sinogram-shaped)
+  float* res;
+};
+
 // Kernel launchers (fp.cu, bp.cu). All return cudaGetLastError() as int.
+// With `sirt` the forward projection writes the SIRT residual instead of sino.
 int launch_fp(const tsgb_projector* p, const float* vol, float* sino, bool additive,
-              float* workspace, void* stream);
+              float* workspace, void* stream, const FpSirt* sirt = nullptr);
 int launch_bp_matched(const tsgb_projector* p, float* vol, const float* sino, bool additive,
                       float* workspace, void* stream);
 int launch_bp_bilinear(const tsgb_projector* p, float* vol, const float* sino, bool additive,
                        float* workspace, void* stream);
 
-// Batched SIRT (batch.cu builds the tables; fp.cu / bp.cu launch).
-struct SirtBatchDev;
-int launch_sirt_fp_batch(const SirtBatchDev& b, void* stream);
-int launch_sirt_bp_batch(const SirtBatchDev& b, void* stream);
+// SIRT update x += C * A^T(res) from a residual written by launch_fp's SIRT
+// epilogue (separable angles only), rounded as the plain recipe's x += C * bp.
+int launch_bp_sirt(const tsgb_projector* p, float* vol, const float* C, const float* res,
+                   void* stream);
 constexpr int kBpRunZ = 16;  // voxels along z per matched-backprojection thread
 constexpr int kBpTileX = 32, kBpTileY = 4, kFpTileRows = 32, kFpTileCols = 8;
 

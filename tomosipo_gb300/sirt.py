@@ -7,13 +7,13 @@ The recipe (``README.md:150-163``, ``doc/intro/fast_reconstruction.rst:92-104``)
     x += C * A.T(R * (y - A(x)))             # per iteration
 
 ``sirt`` runs it exactly like that with the operator and torch element-wise
-ops ("looping the plain operator"). ``BatchedSirt`` runs one iteration of many
-independent jobs (any mix of sizes and geometries) as a handful of kernel
-launches over all jobs, with the residual ``R * (y - A x)`` fused into the
-forward projector's epilogue and ``x += C * A.T(r)`` into the backprojector's;
-an iteration can be captured in a CUDA graph. Both produce the same numbers:
-the fused epilogues use the same operations in the same order, without FMA
-contraction.
+ops ("looping the plain operator"). ``BatchedSirt`` advances many independent
+jobs (any mix of sizes and geometries) together: per job and iteration one
+forward kernel whose epilogue writes the residual ``W R (y - A x)`` and one
+backward kernel whose epilogue applies ``x += C A.T(r)``, with jobs spread
+over concurrent streams and iterations captured in a CUDA graph. Both produce
+the same numbers: the fused epilogues use the same operations in the same
+order, without FMA contraction.
 """
 import ctypes
 
@@ -131,11 +131,14 @@ class BatchedSirt:
 
     ``jobs`` is a list of ``(A, y)`` or ``(A, y, x_init)`` with ``y`` a CUDA
     tensor on one device; jobs may differ in size and geometry (their
-    detectors' v axis must run along z: circular and helical scans). Each
-    iteration is three kernel launches over all jobs. ``run(n, graph=True)``
-    captures one iteration in a CUDA graph and replays it. ``x[i]`` is job i's
-    reconstruction, equal to ``sirt(A_i, y_i, n)``.
+    detectors' v axis must run along z: circular and helical scans).
+    ``run(n, graph=True)`` captures ``graph_iterations`` iterations of all jobs
+    in one CUDA graph (a job's next iteration need not wait for the other
+    jobs) and replays it. ``x[i]`` is job i's reconstruction, equal to
+    ``sirt(A_i, y_i, n)``.
     """
+
+    graph_iterations = 10
 
     def __init__(self, jobs):
         if not jobs:
@@ -146,7 +149,7 @@ class BatchedSirt:
         self.states = [SirtJobState(j[0], j[1], j[2] if len(j) > 2 else None, self.device)
                        for j in jobs]
         self._native = NativeBatch(self.states)
-        self._graph = None
+        self._graphs = {}
 
     @property
     def x(self):
@@ -164,22 +167,29 @@ class BatchedSirt:
         """Queue ``iterations`` iterations on the current stream."""
         self._native.step(iterations)
 
-    def _capture(self):
-        g = torch.cuda.CUDAGraph()
-        with torch.cuda.device(self.device):
-            with torch.cuda.graph(g):
-                self.step(1)
+    def _graph(self, iterations):
+        g = self._graphs.get(iterations)
+        if g is None:
+            g = torch.cuda.CUDAGraph()
+            with torch.cuda.device(self.device):
+                with torch.cuda.graph(g):
+                    self.step(iterations)
+            self._graphs[iterations] = g
         return g
 
     def run(self, num_iterations, graph=True):
-        """Run ``num_iterations`` iterations (graph replays if ``graph``)."""
+        """Run ``num_iterations`` iterations (CUDA graph replays if ``graph``)."""
         if not graph:
             self.step(num_iterations)
             return self.x
-        if self._graph is None:
-            self._graph = self._capture()
-        for _ in range(num_iterations):
-            self._graph.replay()
+        chunk = max(1, min(self.graph_iterations, num_iterations))
+        full, rest = divmod(num_iterations, chunk)
+        if full:
+            g = self._graph(chunk)
+            for _ in range(full):
+                g.replay()
+        if rest:
+            self._graph(rest).replay()
         return self.x
 
     def close(self):
