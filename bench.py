@@ -516,16 +516,21 @@ def run_ours(args, rank, world, local_rank):
     peak, peak_kind = measured_peak_hbm()
     bp_avg = statistics.mean(bp_ms) / 1e3
     fp_avg = statistics.mean(fp_ms) / 1e3
-    dom_name, dom_t = ("bp_matched (weight pass + separable gather)", bp_avg)
+    dom_name, dom_t, dom_key = ("bp_matched (weight pass + separable gather)", bp_avg,
+                                "bp_matched_bytes_per_launch_512")
     if fp_avg > bp_avg:
-        dom_name, dom_t = ("fp (layout copies + ray kernel)", fp_avg)
+        dom_name, dom_t, dom_key = ("fp (layout copies + ray kernel)", fp_avg,
+                                    "fp_bytes_per_launch_512")
     achieved = BYTES_PER_UPDATE * U / dom_t / 1e9
+    # DRAM bytes per call of the dominant kernel(s) from one 1-pass ncu capture
+    # of this workload (profiles/launch_list_cone512_1024.md); other workloads
+    # have no capture.
     traffic = None
     tpath = os.path.join(ROOT, "profiles", "traffic.json")
-    if os.path.exists(tpath):
+    if (N, ANGLES) == (512, 1024) and os.path.exists(tpath):
         try:
             with open(tpath) as f:
-                traffic = json.load(f).get("bp_matched_bytes_per_launch_512")
+                traffic = json.load(f).get(dom_key)
         except (OSError, ValueError):
             traffic = None
     batched = serving = lpd = bilinear = None

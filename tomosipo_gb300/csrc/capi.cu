@@ -86,10 +86,12 @@ int tsgb_projector_create(const tsgb_volume_desc* vol, const tsgb_projection_des
       delete p;
       return fail(TSGB_ERR_INVALID, "volume too large for 32-bit indexing of one padded copy");
     }
-  if (p->g.nz > 65535 || p->g.rows > 4 * 65535 || p->g.cols > 8 * 65535) {
+  if (p->g.nz > 65535 || p->g.ny > 2000000 || p->g.nx > 2000000 || p->g.rows > 4 * 65535 ||
+      p->g.cols > 8 * 65535) {
     delete p;
     return fail(TSGB_ERR_INVALID,
-                "volume z extent must be <= 65535, detector rows <= 262140 and columns <= 524280");
+                "volume z extent must be <= 65535, y and x extents <= 2000000, detector rows "
+                "<= 262140 and columns <= 524280");
   }
   p->tuning = tsgb::default_tuning(p->g);
   cudaError_t e = cudaGetDevice(&p->device);

@@ -49,6 +49,44 @@ __global__ void fp_layout_kernel(const float* __restrict__ vol, float* __restric
   }
 }
 
+// The same copy when the volume's contiguous axis x is d or a (so b, the
+// copy's fastest axis, is strided in the volume): each block transposes a
+// 32 x 32 tile of the (f, b) plane through shared memory, where f is the copy
+// axis that is x in the volume (f_is_d: f = d, else f = a), for one index t
+// of the remaining copy axis per blockIdx.z step. Reads run along x and
+// writes along b, both coalesced. Coordinates are those of the padded copy.
+__global__ void __launch_bounds__(256)
+    fp_layout_transpose_kernel(const float* __restrict__ vol, float* __restrict__ out,
+                               LayoutDev L, long long s_d, long long s_a, long long s_b,
+                               int f_is_d) {
+  __shared__ float tile[32][33];
+  const int n_ap = L.n_a + 2 * kPad, n_bp = L.n_b + 2 * kPad;
+  const int f_ext = f_is_d ? L.n_d : n_ap;
+  const int t_ext = f_is_d ? n_ap : L.n_d;
+  const int f0 = blockIdx.x * 32, b0 = blockIdx.y * 32;
+  for (int t = blockIdx.z; t < t_ext; t += gridDim.z) {
+#pragma unroll
+    for (int r = threadIdx.y; r < 32; r += 8) {
+      const int f = f0 + threadIdx.x, bp = b0 + r;
+      const int k = f_is_d ? f : t, ip = f_is_d ? t : f;
+      const int i = ip - kPad, j = bp - kPad;
+      float v = 0.0f;
+      if (f < f_ext && i >= 0 && i < L.n_a && j >= 0 && j < L.n_b)
+        v = __ldg(vol + k * s_d + i * s_a + j * s_b);
+      tile[r][threadIdx.x] = v;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int r = threadIdx.y; r < 32; r += 8) {
+      const int f = f0 + r, bp = b0 + threadIdx.x;
+      const int k = f_is_d ? f : t, ip = f_is_d ? t : f;
+      if (f < f_ext && bp < n_bp)
+        out[L.offset + ((long long)k * n_ap + ip) * n_bp + bp] = tile[threadIdx.x][r];
+    }
+    __syncthreads();
+  }
+}
+
 // Narrow [klo, khi] (plane coordinates) to planes where X + k m lies in (lo, hi).
 __device__ __forceinline__ void clip_planes(float X, float m, float lo, float hi, float& klo,
                                             float& khi) {
@@ -281,12 +319,22 @@ int launch_fp(const tsgb_projector* p, const float* vol, float* sino, bool addit
   const long long vstride[3] = {(long long)g.ny * g.nx, (long long)g.nx, 1};
   for (int i = 0; i < lt.count; ++i) {
     const Layout& L = p->layouts[i];
-    const long long total = L.n_d * (L.n_a + 2 * kPad) * (L.n_b + 2 * kPad);
-    const int threads = 256;
-    const long long blocks = (total + threads - 1) / threads;
-    const int grid = int(blocks < 152LL * 64 ? blocks : 152LL * 64);
-    fp_layout_kernel<<<grid, threads, 0, stream>>>(vol, workspace, lt.l[i], vstride[L.d],
-                                                  vstride[L.a], vstride[L.b]);
+    if (L.b == 2) {  // b is x: a plain copy reads and writes along x
+      const long long total = L.n_d * (L.n_a + 2 * kPad) * (L.n_b + 2 * kPad);
+      const int threads = 256;
+      const long long blocks = (total + threads - 1) / threads;
+      const int grid = int(blocks < 152LL * 64 ? blocks : 152LL * 64);
+      fp_layout_kernel<<<grid, threads, 0, stream>>>(vol, workspace, lt.l[i], vstride[L.d],
+                                                    vstride[L.a], vstride[L.b]);
+    } else {
+      const int f_is_d = L.d == 2 ? 1 : 0;  // which copy axis is the volume's x
+      const long long f_ext = f_is_d ? L.n_d : L.n_a + 2 * kPad;
+      const long long t_ext = f_is_d ? L.n_a + 2 * kPad : L.n_d;
+      const dim3 grid(unsigned((f_ext + 31) / 32), unsigned((L.n_b + 2 * kPad + 31) / 32),
+                      unsigned(t_ext < 65535 ? t_ext : 65535));
+      fp_layout_transpose_kernel<<<grid, dim3(32, 8), 0, stream>>>(
+          vol, workspace, lt.l[i], vstride[L.d], vstride[L.a], vstride[L.b], f_is_d);
+    }
   }
   const long long per_pair = (long long)((g.rows + kFpRows - 1) / kFpRows) *
                              ((g.cols + kFpCols - 1) / kFpCols);
