@@ -414,6 +414,24 @@ def bench_bilinear_pair(torch, ts, device, x, steps):
             "gups": 2 * N ** 3 * ANGLES / ((fp + bp) / 1e3) / 1e9}
 
 
+def max_over_ranks(value, world, device=None):
+    """The largest of every rank's value (the slowest rank's time); the value
+    itself for one rank. Works over NCCL (CUDA device) and gloo (CPU)."""
+    if world <= 1:
+        return value
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([float(value)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def whole_job_gups(world, updates_per_rank_step, steps, seconds):
+    """GUPS of the whole job: every rank's updates over the slowest rank's time."""
+    return world * updates_per_rank_step * steps / seconds / 1e9
+
+
 def run_ours(args, rank, world, local_rank):
     import torch
     import torch.distributed as dist
@@ -468,12 +486,9 @@ def run_ours(args, rank, world, local_rank):
     fp_ms = [e[0].elapsed_time(e[1]) for e in ev]
     bp_ms = [e[1].elapsed_time(e[2]) for e in ev]
 
-    if world > 1:
-        t = torch.tensor([total_ms], device=device)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        total_ms = float(t.item())
+    total_ms = max_over_ranks(total_ms, world, device)
     ms_per_step = total_ms / args.steps
-    value = world * 2 * U * args.steps / (total_ms / 1e3) / 1e9
+    value = whole_job_gups(world, 2 * U, args.steps, total_ms / 1e3)
 
     # End to end through the public API with pinned host buffers: every step
     # copies the volume in, projects, copies the sinogram out, copies it back
@@ -493,16 +508,12 @@ def run_ours(args, rank, world, local_rank):
             A(xh, out=yh)
             A.T(yh, out=vh)
         torch.cuda.synchronize()
-        dt = time.perf_counter() - t0
-        if world > 1:
-            t = torch.tensor([dt], device=device)
-            dist.all_reduce(t, op=dist.ReduceOp.MAX)
-            dt = float(t.item())
+        dt = max_over_ranks(time.perf_counter() - t0, world, device)
         barrier()
         vol_b = 4 * N ** 3
         sino_b = 4 * DET[0] * DET[1] * ANGLES
         e2e = {
-            "value": world * 2 * U * args.steps / dt / 1e9,
+            "value": whole_job_gups(world, 2 * U, args.steps, dt),
             "unit": "GUPS",
             "h2d_bytes_per_step": vol_b + sino_b,
             "d2h_bytes_per_step": sino_b + vol_b,
