@@ -160,7 +160,9 @@ typedef struct {
   int32_t fp_patch_rows;  /* tiles of 32 detector rows per patch (>= 1) */
   int32_t fp_patch_cols;  /* tiles of 8 detector columns per patch (>= 1) */
   int32_t fp_group_pairs; /* pairs of adjacent angles per group (>= 1) */
-  int32_t reserved[5];    /* must be 0 */
+  int32_t fp_pair_layout; /* 1: volume copies hold neighbour pairs (two 8-byte
+                             loads per sample), 0: single voxels (four 4-byte) */
+  int32_t reserved[4];    /* must be 0 */
 } tsgb_tuning;
 
 int tsgb_projector_get_tuning(const tsgb_projector* p, tsgb_tuning* out);

@@ -1,7 +1,7 @@
 """Forward-projector schedules (tsgb_tuning) and the autotuner.
 
-The schedule only orders independent tiles, so every tuning must give
-bit-identical sinograms, on detectors whose sizes are not multiples of the
+The schedule only orders independent tiles and both copy layouts feed the
+same arithmetic, so every tuning must give bit-identical sinograms, on detectors whose sizes are not multiples of the
 tile and with odd angle counts (ragged last patch, strip, group and pair).
 """
 import ctypes
@@ -18,10 +18,10 @@ torch = pytest.importorskip("torch")
 pytestmark = pytest.mark.gpu
 
 TUNINGS = [
-    dict(fp_patch_rows=1, fp_patch_cols=1, fp_group_pairs=1),
-    dict(fp_patch_rows=3, fp_patch_cols=5, fp_group_pairs=2),
-    dict(fp_patch_rows=2, fp_patch_cols=64, fp_group_pairs=7),
-    dict(fp_patch_rows=16, fp_patch_cols=3, fp_group_pairs=1000),
+    dict(fp_patch_rows=1, fp_patch_cols=1, fp_group_pairs=1, fp_pair_layout=0),
+    dict(fp_patch_rows=3, fp_patch_cols=5, fp_group_pairs=2, fp_pair_layout=1),
+    dict(fp_patch_rows=2, fp_patch_cols=64, fp_group_pairs=7, fp_pair_layout=0),
+    dict(fp_patch_rows=16, fp_patch_cols=3, fp_group_pairs=1000, fp_pair_layout=1),
 ]
 
 
@@ -68,7 +68,8 @@ def test_set_tuning_rejects_bad_values(dev):
     A = ts.operator(ts.volume(shape=8, size=1), ts.cone(angles=3, shape=(8, 8), cone_angle=0.3))
     h = A.projector.handle(dev.index)
     lib = _native.load()
-    for bad in (dict(fp_patch_rows=0), dict(fp_patch_cols=-1), dict(fp_group_pairs=0)):
+    for bad in (dict(fp_patch_rows=0), dict(fp_patch_cols=-1), dict(fp_group_pairs=0),
+                dict(fp_pair_layout=2)):
         t = _native.Tuning(**dict(dict(fp_patch_rows=1, fp_patch_cols=1, fp_group_pairs=1), **bad))
         assert lib.tsgb_projector_set_tuning(h, ctypes.byref(t)) == -1
     t = _native.Tuning(fp_patch_rows=1, fp_patch_cols=1, fp_group_pairs=1)

@@ -51,7 +51,8 @@ class Tuning(ctypes.Structure):
         ("fp_patch_rows", ctypes.c_int32),
         ("fp_patch_cols", ctypes.c_int32),
         ("fp_group_pairs", ctypes.c_int32),
-        ("reserved", ctypes.c_int32 * 5),
+        ("fp_pair_layout", ctypes.c_int32),
+        ("reserved", ctypes.c_int32 * 4),
     ]
 
 

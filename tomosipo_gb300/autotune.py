@@ -4,12 +4,14 @@ The forward projector runs its tiles (32 detector rows x 8 columns of one
 pair of adjacent angles) in an order set by three numbers (``tsgb_tuning``):
 detector patches of ``fp_patch_rows`` x ``fp_patch_cols`` tiles and groups of
 ``fp_group_pairs`` angle pairs. A group's tiles over one patch run together,
-so the volume slab their rays cross stays in L2 across the group's angles.
-The best values depend on the volume and detector sizes and on the cone
-angle. ``autotune(A)`` times ``A``'s forward projection under candidate
-schedules with CUDA events (coordinate descent from the default: patch
-rows, then group size, then patch columns, each from the best so far) and
-sets the fastest on the operator's projector. The batched SIRT solver launches each job's tiles in its
+so the volume slab their rays cross stays in L2 across the group's angles. A
+fourth, ``fp_pair_layout``, stores the padded volume copies as neighbour
+pairs (two 8-byte loads per bilinear sample instead of four 4-byte ones, at
+twice the footprint). The best values depend on the volume and detector
+sizes and on the cone angle. ``autotune(A)`` times ``A``'s forward
+projection under candidate settings with CUDA events (coordinate descent from
+the default: element layout, patch rows, group size, patch columns, each from
+the best so far) and sets the fastest on the operator's projector. The batched SIRT solver launches each job's tiles in its
 projector's order, so tuning a job's operator tunes its part of the batch.
 
 Every schedule gives bit-identical results: only the order of independent
@@ -24,6 +26,7 @@ import os
 
 import torch
 
+PAIR_LAYOUT = (0, 1)
 PATCH_ROWS = (2, 4, 8, 16, 32)
 GROUP_PAIRS = (8, 16, 32, 64, 128)
 PATCH_COLS = (1, 2, 4, 8, 16)
@@ -89,8 +92,8 @@ def autotune(A, device=None, repeats=None, cache_path=None, verbose=False):
         best = proj.get_tuning(dev.index)
         best_ms = _time_fp(A, x, y, reps)
         default_ms, trials = best_ms, 1
-        for name, values in (("fp_patch_rows", PATCH_ROWS), ("fp_group_pairs", GROUP_PAIRS),
-                             ("fp_patch_cols", PATCH_COLS)):
+        for name, values in (("fp_pair_layout", PAIR_LAYOUT), ("fp_patch_rows", PATCH_ROWS),
+                             ("fp_group_pairs", GROUP_PAIRS), ("fp_patch_cols", PATCH_COLS)):
             for v in values:
                 if v == best[name]:
                     continue

@@ -124,12 +124,16 @@ __device__ __forceinline__ void bp_separable_accumulate(
       if (fabsf(Sl) >= 1.0f) {
         // Tent half-width 1/|Sl| <= 1 row: only rows floor(v*) and floor(v*)+1.
         // Voxel j's row position vs = (z_j - B) / Sl; row v0's ray passes the
-        // plane at q_b - z_j = v0 Sl + (B - zt0) - j. The column weight h is
-        // folded into the tents: h tent(t) = max(0, h - h |t|).
+        // plane at t0 = q_b - z_j = v0 Sl + (B - zt0) - j = -Sl (vs - v0), and
+        // row v0+1's at t0 + Sl, so |t0 + Sl| = |Sl| - |t0| for the rows the
+        // run selects. The column weight h is folded into the tents:
+        //   h tent(t0) = max(0, h - h |t0|),
+        //   h tent(t0 + Sl) = max(0, h (1 - |Sl|) + h |t0|).
         const float vs0 = (zt0 - B) * inv;
         const float vs1 = fmaf(float(kRun - 1), inv, vs0);
         const float C0 = B - zt0;
         const float nh = -h;
+        const float h1 = h - h * fabsf(Sl);
         const float2* __restrict__ colv = col + Offset(g.ov) * rs;  // row 0 of this column
         // vs is monotone in j: if both ends select rows inside [vmin, vmax]
         // every voxel does, and no clamping is needed (NaN fails the test).
@@ -139,8 +143,9 @@ __device__ __forceinline__ void bp_separable_accumulate(
             const float v0 = floorf(fmaf(float(j), inv, vs0));
             const float t0 = fmaf(v0, Sl, C0) - float(j);
             const float2 yy = __ldg(colv + Offset((int)v0) * rs);
-            acc[j] = fmaf(fmaxf(0.0f, fmaf(nh, fabsf(t0), h)), yy.x,
-                          fmaf(fmaxf(0.0f, fmaf(nh, fabsf(t0 + Sl), h)), yy.y, acc[j]));
+            const float at0 = fabsf(t0);
+            acc[j] = fmaf(fmaxf(0.0f, fmaf(nh, at0, h)), yy.x,
+                          fmaf(fmaxf(0.0f, fmaf(h, at0, h1)), yy.y, acc[j]));
           }
         } else {
 #pragma unroll
@@ -150,8 +155,9 @@ __device__ __forceinline__ void bp_separable_accumulate(
             const float v0 = fminf(fmaxf(floorf(fmaf(float(j), inv, vs0)), vmin), vmax);
             const float t0 = fmaf(v0, Sl, C0) - float(j);
             const float2 yy = __ldg(colv + Offset((int)v0) * rs);
-            acc[j] = fmaf(fmaxf(0.0f, fmaf(nh, fabsf(t0), h)), yy.x,
-                          fmaf(fmaxf(0.0f, fmaf(nh, fabsf(t0 + Sl), h)), yy.y, acc[j]));
+            const float at0 = fabsf(t0);
+            acc[j] = fmaf(fmaxf(0.0f, fmaf(nh, at0, h)), yy.x,
+                          fmaf(fmaxf(0.0f, fmaf(h, at0, h1)), yy.y, acc[j]));
           }
         }
       } else {

@@ -82,7 +82,7 @@ int tsgb_projector_create(const tsgb_volume_desc* vol, const tsgb_projection_des
     return fail(TSGB_ERR_INVALID, err);
   }
   for (const auto& L : p->layouts)
-    if (L.floats() >= (int64_t(1) << 31)) {
+    if (L.elems() >= (int64_t(1) << 31)) {
       delete p;
       return fail(TSGB_ERR_INVALID, "volume too large for 32-bit indexing of one padded copy");
     }
@@ -93,7 +93,7 @@ int tsgb_projector_create(const tsgb_volume_desc* vol, const tsgb_projection_des
                 "volume z extent must be <= 65535, y and x extents <= 2000000, detector rows "
                 "<= 262140 and columns <= 524280");
   }
-  p->tuning = tsgb::default_tuning(p->g);
+  p->tuning = tsgb::default_tuning(p);
   cudaError_t e = cudaGetDevice(&p->device);
   if (e == cudaSuccess) e = upload(&p->d_params, p->host_params);
   if (e == cudaSuccess) e = upload(&p->d_columns, columns);
@@ -124,7 +124,7 @@ int tsgb_projector_destroy(tsgb_projector* p) {
 
 int64_t tsgb_fp_workspace_bytes(const tsgb_projector* p) {
   if (!p) return fail(TSGB_ERR_INVALID, "projector is NULL");
-  return p->fp_workspace_floats * int64_t(sizeof(float));
+  return p->fp_workspace_elems * int64_t(2 * sizeof(float));  // pairs of floats
 }
 
 int64_t tsgb_bp_workspace_bytes(const tsgb_projector* p, int32_t bp_kind) {
@@ -224,7 +224,9 @@ int tsgb_projector_set_tuning(tsgb_projector* p, const tsgb_tuning* t) {
   if (!p || !t) return fail(TSGB_ERR_INVALID, "projector or tuning is NULL");
   if (t->fp_patch_rows < 1 || t->fp_patch_cols < 1 || t->fp_group_pairs < 1)
     return fail(TSGB_ERR_INVALID, "tuning values must be >= 1");
-  for (int i = 0; i < 5; ++i)
+  if (t->fp_pair_layout != 0 && t->fp_pair_layout != 1)
+    return fail(TSGB_ERR_INVALID, "fp_pair_layout must be 0 or 1");
+  for (int i = 0; i < 4; ++i)
     if (t->reserved[i] != 0) return fail(TSGB_ERR_INVALID, "reserved tuning fields must be 0");
   p->tuning = *t;
   return TSGB_OK;

@@ -28,7 +28,7 @@ __host__ inline LayoutTable make_layout_table(const tsgb_projector* p) {
   for (int i = 0; i < t.count; ++i) {
     const Layout& L = p->layouts[i];
     LayoutDev& D = t.l[i];
-    D.offset = L.offset_floats;
+    D.offset = L.offset_elems;
     D.n_d = int(L.n_d);
     D.n_a = int(L.n_a);
     D.n_b = int(L.n_b);

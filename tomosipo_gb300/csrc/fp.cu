@@ -31,7 +31,33 @@ constexpr int kFpCols = kFpTileCols;  // warps along detector columns
 // (both here and, through the weighted sinogram, in the transpose).
 constexpr float kMaxSlope = 64.0f;
 
-__global__ void fp_layout_kernel(const float* __restrict__ vol, float* __restrict__ out,
+// Padded copy c of the volume in an angle's [d][a][b] frame, c = 0 in the
+// kPad-wide border (and past its far edge), stored as single voxels or as
+// pairs along b: element (k, ip, jp) = (c[k][ip][jp], c[k][ip][jp+1]). Used
+// when b is the volume's x, so reads and writes both run along x.
+__device__ __forceinline__ float padded_voxel(const float* __restrict__ vol, const LayoutDev& L,
+                                              long long k, long long ip, long long jp,
+                                              long long s_d, long long s_a, long long s_b) {
+  const long long i = ip - kPad, j = jp - kPad;
+  if (i < 0 || i >= L.n_a || j < 0 || j >= L.n_b) return 0.0f;
+  return __ldg(vol + k * s_d + i * s_a + j * s_b);
+}
+
+// Element of a padded copy: one voxel (float) or the pair (c[j], c[j+1]) along b
+// (float2), as the projector's tuning chooses.
+template <typename E>
+__device__ __forceinline__ E copy_elem(float a, float b);
+template <>
+__device__ __forceinline__ float copy_elem<float>(float a, float) {
+  return a;
+}
+template <>
+__device__ __forceinline__ float2 copy_elem<float2>(float a, float b) {
+  return make_float2(a, b);
+}
+
+template <typename E>
+__global__ void fp_layout_kernel(const float* __restrict__ vol, E* __restrict__ out,
                                  LayoutDev L, long long s_d, long long s_a, long long s_b) {
   const long long n_ap = L.n_a + 2 * kPad;
   const long long n_bp = L.n_b + 2 * kPad;
@@ -42,31 +68,30 @@ __global__ void fp_layout_kernel(const float* __restrict__ vol, float* __restric
     const long long rest = idx / n_bp;
     const long long ip = rest % n_ap;
     const long long k = rest / n_ap;
-    const long long i = ip - kPad, j = jp - kPad;
-    float v = 0.0f;
-    if (i >= 0 && i < L.n_a && j >= 0 && j < L.n_b) v = __ldg(vol + k * s_d + i * s_a + j * s_b);
-    out[L.offset + idx] = v;
+    out[L.offset + idx] = copy_elem<E>(padded_voxel(vol, L, k, ip, jp, s_d, s_a, s_b),
+                                       padded_voxel(vol, L, k, ip, jp + 1, s_d, s_a, s_b));
   }
 }
 
 // The same copy when the volume's contiguous axis x is d or a (so b, the
 // copy's fastest axis, is strided in the volume): each block transposes a
-// 32 x 32 tile of the (f, b) plane through shared memory, where f is the copy
+// 32 x 33 tile of the (f, b) plane through shared memory, where f is the copy
 // axis that is x in the volume (f_is_d: f = d, else f = a), for one index t
-// of the remaining copy axis per blockIdx.z step. Reads run along x and
+// of the remaining copy axis per blockIdx.z step, and writes 32 elements
+// along b (the 33rd b value is the last pair's second half). Reads run along x and
 // writes along b, both coalesced. Coordinates are those of the padded copy.
+template <typename E>
 __global__ void __launch_bounds__(256)
-    fp_layout_transpose_kernel(const float* __restrict__ vol, float* __restrict__ out,
+    fp_layout_transpose_kernel(const float* __restrict__ vol, E* __restrict__ out,
                                LayoutDev L, long long s_d, long long s_a, long long s_b,
                                int f_is_d) {
-  __shared__ float tile[32][33];
+  __shared__ float tile[33][33];  // [b][f]
   const int n_ap = L.n_a + 2 * kPad, n_bp = L.n_b + 2 * kPad;
   const int f_ext = f_is_d ? L.n_d : n_ap;
   const int t_ext = f_is_d ? n_ap : L.n_d;
   const int f0 = blockIdx.x * 32, b0 = blockIdx.y * 32;
   for (int t = blockIdx.z; t < t_ext; t += gridDim.z) {
-#pragma unroll
-    for (int r = threadIdx.y; r < 32; r += 8) {
+    for (int r = threadIdx.y; r < 33; r += 8) {
       const int f = f0 + threadIdx.x, bp = b0 + r;
       const int k = f_is_d ? f : t, ip = f_is_d ? t : f;
       const int i = ip - kPad, j = bp - kPad;
@@ -81,7 +106,8 @@ __global__ void __launch_bounds__(256)
       const int f = f0 + r, bp = b0 + threadIdx.x;
       const int k = f_is_d ? f : t, ip = f_is_d ? t : f;
       if (f < f_ext && bp < n_bp)
-        out[L.offset + ((long long)k * n_ap + ip) * n_bp + bp] = tile[threadIdx.x][r];
+        out[L.offset + ((long long)k * n_ap + ip) * n_bp + bp] =
+            copy_elem<E>(tile[threadIdx.x][r], tile[threadIdx.x + 1][r]);
     }
     __syncthreads();
   }
@@ -101,6 +127,7 @@ __device__ __forceinline__ void clip_planes(float X, float m, float lo, float hi
   }
 }
 
+// Bilinear sample of plane k from single voxels (four 4-byte taps) ...
 __device__ __forceinline__ float bilinear_sample(const float* __restrict__ base, const Ray& r,
                                                  int k, int stride_d, int stride_a) {
   const float kt = float(k);
@@ -116,14 +143,32 @@ __device__ __forceinline__ float bilinear_sample(const float* __restrict__ base,
   return fmaf(fa, right - left, left);
 }
 
+// ... or from pairs (two 8-byte taps, each holding both b neighbours); the
+// arithmetic is the same, so both give identical results.
+__device__ __forceinline__ float bilinear_sample(const float2* __restrict__ base, const Ray& r,
+                                                 int k, int stride_d, int stride_a) {
+  const float kt = float(k);
+  const float qa = fmaf(kt, r.ma, r.Xa);
+  const float qb = fmaf(kt, r.mb, r.Xb);
+  const float fa0 = floorf(qa), fb0 = floorf(qb);
+  const float fa = qa - fa0, fb = qb - fb0;
+  const float2* p = base + (k * stride_d + (int)fa0 * stride_a + (int)fb0);
+  const float2 v0 = __ldg(p), v1 = __ldg(p + stride_a);
+  const float left = fmaf(fb, v0.y - v0.x, v0.x);
+  const float right = fmaf(fb, v1.y - v1.x, v1.x);
+  return fmaf(fa, right - left, left);
+}
+
 // The padded volume copy an angle samples: anchored voxel (0, 0, 0) and strides.
+template <typename E>
 struct CopyView {
-  const float* base;
+  const E* base;
   int stride_d, stride_a;
 };
 
-__device__ __forceinline__ CopyView copy_view(const AngleParams& ap, const float* __restrict__ ws) {
-  CopyView v;
+template <typename E>
+__device__ __forceinline__ CopyView<E> copy_view(const AngleParams& ap, const E* __restrict__ ws) {
+  CopyView<E> v;
   v.stride_d = ap.stride_d;
   v.stride_a = ap.stride_a;
   v.base = ws + ap.ws_offset + (long long)ap.o_d * ap.stride_d +
@@ -169,14 +214,16 @@ __device__ __forceinline__ RaySpan prepare_span(const AngleParams& ap,
   return s;
 }
 
-__device__ __forceinline__ float sample(const CopyView& v, const Ray& r, int k) {
+template <typename E>
+__device__ __forceinline__ float sample(const CopyView<E>& v, const Ray& r, int k) {
   return bilinear_sample(v.base, r, k, v.stride_d, v.stride_a);
 }
 
 // Samples of planes k0..k1 are summed into two partial sums by the parity of
 // k (even planes into e, odd into o), in increasing k, so a ray's result does
 // not depend on how its planes are scheduled against another ray's.
-__device__ __forceinline__ void walk(const CopyView& v, const Ray& r, int k0, int k1, float& e,
+template <typename E>
+__device__ __forceinline__ void walk(const CopyView<E>& v, const Ray& r, int k0, int k1, float& e,
                                      float& o) {
   int k = k0;
   if (k <= k1 && (k & 1)) o += sample(v, r, k++);
@@ -190,9 +237,10 @@ __device__ __forceinline__ void walk(const CopyView& v, const Ray& r, int k0, in
 // Ray sum (scaled by the plane step) of pixel (iv, iu) at angle theta. If W
 // is given it receives ray_weight. Values needed only after the plane loop
 // are computed after it, which keeps registers free for loads in flight.
+template <typename E>
 __device__ __forceinline__ float fp_ray_total(const AngleParams& ap,
                                               const ColumnEntry* __restrict__ columns,
-                                              const float* __restrict__ ws,
+                                              const E* __restrict__ ws,
                                               const DeviceGeometry& g, int iv, int iu, int theta,
                                               float* W) {
   const RaySpan s = prepare_span(ap, columns, g, iv, iu, theta);
@@ -206,14 +254,15 @@ __device__ __forceinline__ float fp_ray_total(const AngleParams& ap,
 // planes are walked together through one base pointer and one set of strides,
 // so the second ray's taps (near the first's) hit lines the first just
 // brought into L1. Results equal fp_ray_total's.
+template <typename E>
 __device__ __forceinline__ void fp_ray_pair(const AngleParams& apa, const AngleParams& apb,
                                             const ColumnEntry* __restrict__ columns,
-                                            const float* __restrict__ ws,
+                                            const E* __restrict__ ws,
                                             const DeviceGeometry& g, int iv, int iu, int theta,
                                             float& ta, float& tb, float* Wa, float* Wb) {
   const RaySpan a = prepare_span(apa, columns, g, iv, iu, theta);
   const RaySpan b = prepare_span(apb, columns, g, iv, iu, theta + 1);
-  const CopyView va = copy_view(apa, ws);
+  const CopyView<E> va = copy_view(apa, ws);
   float ea = 0.0f, oa = 0.0f, eb = 0.0f, ob = 0.0f;
   const int lo = max(a.k0, b.k0), hi = min(a.k1, b.k1);
   if (apa.layout == apb.layout && lo <= hi) {
@@ -270,10 +319,11 @@ __device__ __forceinline__ void sirt_residual(const FpSirt& s, const DeviceGeome
 // kept in registers across it). Four resident blocks per SM leave 64
 // registers a thread, which the plane loop spends on loads in flight.
 // kSirt: write the SIRT residual (sirt_residual) instead of the sinogram.
-template <bool kSirt>
+// E: the copies' element type (float: single voxels, float2: pairs along b).
+template <bool kSirt, typename E>
 __global__ void __launch_bounds__(kFpRows* kFpCols, 4)
     fp_ray_kernel(const AngleParams* __restrict__ params, const ColumnEntry* __restrict__ columns,
-                  const float* __restrict__ ws, float* __restrict__ sino, DeviceGeometry g,
+                  const E* __restrict__ ws, float* __restrict__ sino, DeviceGeometry g,
                   FpSchedule sched, int angle0, int additive, FpSirt sirt) {
   __shared__ volatile long long out_slot[kFpRows * kFpCols];
   int rb, cb, pr;
@@ -311,9 +361,13 @@ __global__ void __launch_bounds__(kFpRows* kFpCols, 4)
 
 }  // namespace
 
-int launch_fp(const tsgb_projector* p, const float* vol, float* sino, bool additive,
-              float* workspace, void* stream_, const FpSirt* sirt) {
-  cudaStream_t stream = static_cast<cudaStream_t>(stream_);
+namespace {
+
+// Volume copies and ray kernels with copy elements of type E (offsets and
+// strides count elements, so both types use the same plan).
+template <typename E>
+void launch_fp_elems(const tsgb_projector* p, const float* vol, float* sino, bool additive,
+                     E* copies, cudaStream_t stream, const FpSirt* sirt) {
   const DeviceGeometry& g = p->g;
   const LayoutTable lt = make_layout_table(p);
   const long long vstride[3] = {(long long)g.ny * g.nx, (long long)g.nx, 1};
@@ -324,16 +378,16 @@ int launch_fp(const tsgb_projector* p, const float* vol, float* sino, bool addit
       const int threads = 256;
       const long long blocks = (total + threads - 1) / threads;
       const int grid = int(blocks < 152LL * 64 ? blocks : 152LL * 64);
-      fp_layout_kernel<<<grid, threads, 0, stream>>>(vol, workspace, lt.l[i], vstride[L.d],
-                                                    vstride[L.a], vstride[L.b]);
+      fp_layout_kernel<E><<<grid, threads, 0, stream>>>(vol, copies, lt.l[i], vstride[L.d],
+                                                       vstride[L.a], vstride[L.b]);
     } else {
       const int f_is_d = L.d == 2 ? 1 : 0;  // which copy axis is the volume's x
       const long long f_ext = f_is_d ? L.n_d : L.n_a + 2 * kPad;
       const long long t_ext = f_is_d ? L.n_a + 2 * kPad : L.n_d;
       const dim3 grid(unsigned((f_ext + 31) / 32), unsigned((L.n_b + 2 * kPad + 31) / 32),
                       unsigned(t_ext < 65535 ? t_ext : 65535));
-      fp_layout_transpose_kernel<<<grid, dim3(32, 8), 0, stream>>>(
-          vol, workspace, lt.l[i], vstride[L.d], vstride[L.a], vstride[L.b], f_is_d);
+      fp_layout_transpose_kernel<E><<<grid, dim3(32, 8), 0, stream>>>(
+          vol, copies, lt.l[i], vstride[L.d], vstride[L.a], vstride[L.b], f_is_d);
     }
   }
   const long long per_pair = (long long)((g.rows + kFpRows - 1) / kFpRows) *
@@ -344,12 +398,23 @@ int launch_fp(const tsgb_projector* p, const float* vol, float* sino, bool addit
     const FpSchedule s = fp_schedule(p, (n + 1) / 2);
     const long long blocks = per_pair * s.pairs;
     if (sirt)
-      fp_ray_kernel<true><<<unsigned(blocks), dim3(kFpRows, kFpCols), 0, stream>>>(
-          p->d_params, p->d_columns, workspace, sino, g, s, int(a0), 0, *sirt);
+      fp_ray_kernel<true, E><<<unsigned(blocks), dim3(kFpRows, kFpCols), 0, stream>>>(
+          p->d_params, p->d_columns, copies, sino, g, s, int(a0), 0, *sirt);
     else
-      fp_ray_kernel<false><<<unsigned(blocks), dim3(kFpRows, kFpCols), 0, stream>>>(
-          p->d_params, p->d_columns, workspace, sino, g, s, int(a0), additive ? 1 : 0, FpSirt{});
+      fp_ray_kernel<false, E><<<unsigned(blocks), dim3(kFpRows, kFpCols), 0, stream>>>(
+          p->d_params, p->d_columns, copies, sino, g, s, int(a0), additive ? 1 : 0, FpSirt{});
   }
+}
+
+}  // namespace
+
+int launch_fp(const tsgb_projector* p, const float* vol, float* sino, bool additive,
+              float* workspace, void* stream_, const FpSirt* sirt) {
+  cudaStream_t stream = static_cast<cudaStream_t>(stream_);
+  if (p->tuning.fp_pair_layout)
+    launch_fp_elems(p, vol, sino, additive, reinterpret_cast<float2*>(workspace), stream, sirt);
+  else
+    launch_fp_elems(p, vol, sino, additive, workspace, stream, sirt);
   return int(cudaGetLastError());
 }
 
@@ -372,8 +437,15 @@ FpSchedule fp_schedule(const tsgb_projector* p, int pairs) {
   return s;
 }
 
-tsgb_tuning default_tuning(const DeviceGeometry&) {
+tsgb_tuning default_tuning(const tsgb_projector* p) {
   tsgb_tuning t{};
+  // Pairs along b halve the sampler's load instructions (the gather is bound
+  // by L1 wavefronts) but double the copies' footprint: at 256^3 they are 11 %
+  // faster, at 512^3 (a 1.1 GB pair copy) 12 % slower because the schedule's
+  // volume slab then spills L2. Default: pairs while a pair copy is <= 512 MB.
+  int64_t largest = 0;
+  for (const auto& L : p->layouts) largest = std::max<int64_t>(largest, L.elems());
+  t.fp_pair_layout = largest * 8 <= (int64_t(512) << 20) ? 1 : 0;
   // Patches of 256 detector rows x 32 columns and groups of 64 angles: the
   // volume slab such a group crosses stays in L2 while it runs (fastest on a
   // 512^3 cone scan with a 512 x 768 detector and 1024 angles, and within

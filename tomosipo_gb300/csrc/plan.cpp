@@ -248,7 +248,7 @@ std::string build_plan(const tsgb_volume_desc* vol, const tsgb_projection_desc* 
       L.n_d = shape[d];
       L.n_a = shape[a];
       L.n_b = shape[b];
-      L.offset_floats = 0;
+      L.offset_elems = 0;
       p->layouts.push_back(L);
       li = int(p->layouts.size()) - 1;
     }
@@ -277,12 +277,12 @@ std::string build_plan(const tsgb_volume_desc* vol, const tsgb_projection_desc* 
 
   int64_t off = 0;
   for (auto& L : p->layouts) {
-    L.offset_floats = off;
-    off += (L.floats() + 63) / 64 * 64;  // keep every copy 256-byte aligned
+    L.offset_elems = off;
+    off += (L.elems() + 31) / 32 * 32;  // keep every copy 256-byte aligned
   }
   for (auto& ap : p->host_params) {
     const Layout& L = p->layouts[ap.layout];
-    ap.ws_offset = L.offset_floats;
+    ap.ws_offset = L.offset_elems;
     ap.n_d = int(L.n_d);
     ap.n_a = int(L.n_a);
     ap.n_b = int(L.n_b);
@@ -295,7 +295,7 @@ std::string build_plan(const tsgb_volume_desc* vol, const tsgb_projection_desc* 
     ap.vs_a = float(vs[L.a]);
     ap.vs_b = float(vs[L.b]);
   }
-  p->fp_workspace_floats = off;
+  p->fp_workspace_elems = off;
   p->n_general_bp = int(gen_angles->size());
   p->n_separable_bp = int(sep_angles->size());
   p->n_bil_fast = int(bil_fast->size());

@@ -74,8 +74,13 @@ struct alignas(16) ColumnEntry {
 struct Layout {
   int d, a, b;
   int64_t n_d, n_a, n_b;   // unpadded extents
-  int64_t offset_floats;   // offset of this copy in the forward workspace
-  int64_t floats() const { return n_d * (n_a + 2 * kPad) * (n_b + 2 * kPad); }
+  // The forward workspace holds the copies as single voxels or, with the
+  // tuning's fp_pair_layout, as pairs along b: element (k, i, j) =
+  // (c[k][i][j], c[k][i][j+1]) of the padded copy c, so a bilinear sample is
+  // two 8-byte loads. Offsets and sizes count elements; the workspace is sized
+  // for pairs either way.
+  int64_t offset_elems;   // offset of this copy in the forward workspace
+  int64_t elems() const { return n_d * (n_a + 2 * kPad) * (n_b + 2 * kPad); }
 };
 
 struct DeviceGeometry {
@@ -104,7 +109,7 @@ struct tsgb_projector {
   tsgb_tuning tuning;
   std::vector<tsgb::AngleParams> host_params;
   std::vector<tsgb::Layout> layouts;
-  int64_t fp_workspace_floats = 0;
+  int64_t fp_workspace_elems = 0;  // 8-byte pair elements
   int n_general_bp = 0;         // angles handled by the general BP kernel
   int n_separable_bp = 0;       // angles handled by the separable BP kernel
   int n_bil_fast = 0;           // bilinear BP: angles for the z-flat kernel
@@ -132,8 +137,8 @@ std::string build_plan(const tsgb_volume_desc* vol, const tsgb_projection_desc* 
 FpSchedule fp_schedule(const tsgb_projector* p, int pairs);
 // Angles per forward-projection launch (fp.cu).
 long long fp_angle_chunk(const DeviceGeometry& g);
-// Default tuning of a new projector (fp.cu).
-tsgb_tuning default_tuning(const DeviceGeometry& g);
+// Default tuning of a new projector whose plan is built (fp.cu).
+tsgb_tuning default_tuning(const tsgb_projector* p);
 
 // Sets the calling thread's message returned by tsgb_last_error (capi.cu).
 void set_last_error(const std::string& msg);

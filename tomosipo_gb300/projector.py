@@ -98,7 +98,7 @@ class Projector:
                 "bp_workspace_bytes"]
         return dict(zip(keys, [int(v) for v in out]))
 
-    TUNING_KEYS = ("fp_patch_rows", "fp_patch_cols", "fp_group_pairs")
+    TUNING_KEYS = ("fp_patch_rows", "fp_patch_cols", "fp_group_pairs", "fp_pair_layout")
 
     def get_tuning(self, device_index=None):
         """Launch schedule of the forward projector (see tsgb_tuning)."""
