@@ -363,7 +363,20 @@ __global__ void __launch_bounds__(kBpX* kBpY)
 
 // Copy the sinogram into a layout with kRowPad zero rows above and below and
 // kColPad zero columns left and right of the detector.
-__global__ void bp_bilinear_prep_kernel(const float* __restrict__ sino, float* __restrict__ out,
+// Detector value at (iv, iu) of angle t, zero outside the detector.
+__device__ __forceinline__ float detector_or_zero(const float* __restrict__ sino,
+                                                  const DeviceGeometry& g, long long iv,
+                                                  long long t, long long iu) {
+  if (iu < 0 || iu >= g.cols || iv < 0 || iv >= g.rows) return 0.0f;
+  return __ldg(sino + ((size_t)iv * g.nangles + t) * g.cols + iu);
+}
+
+// Quad copy of the sinogram for bp_bilinear_z_kernel: element (iv, t, iu) for
+// iv in -kRowPad .. rows + kRowPad - 1 and iu in -kColPad .. cols + kColPad - 1
+// holds the four taps of a bilinear read, (y[iv][iu], y[iv][iu+1],
+// y[iv+1][iu], y[iv+1][iu+1]), zero outside the detector, so one 16-byte
+// load serves a voxel.
+__global__ void bp_bilinear_prep_kernel(const float* __restrict__ sino, float4* __restrict__ out,
                                         DeviceGeometry g) {
   const long long cp = g.cols + 2 * kColPad, rp = g.rows + 2 * kRowPad;
   const long long total = rp * g.nangles * cp;
@@ -372,10 +385,10 @@ __global__ void bp_bilinear_prep_kernel(const float* __restrict__ sino, float* _
     const long long c = idx % cp, rest = idx / cp;
     const long long t = rest % g.nangles, r = rest / g.nangles;
     const long long iu = c - kColPad, iv = r - kRowPad;
-    float v = 0.0f;
-    if (iu >= 0 && iu < g.cols && iv >= 0 && iv < g.rows)
-      v = __ldg(sino + ((size_t)iv * g.nangles + t) * g.cols + iu);
-    out[idx] = v;
+    out[idx] = make_float4(detector_or_zero(sino, g, iv, t, iu),
+                           detector_or_zero(sino, g, iv, t, iu + 1),
+                           detector_or_zero(sino, g, iv + 1, t, iu),
+                           detector_or_zero(sino, g, iv + 1, t, iu + 1));
   }
 }
 
@@ -383,24 +396,24 @@ __global__ void bp_bilinear_prep_kernel(const float* __restrict__ sino, float* _
 // projective denominator constant along z (det_v along z). A thread owns a
 // voxel column (x, y) and kRun voxels along z: per angle it projects the
 // column once (detector column pair, 1/w, the distance weight's horizontal
-// part), then per voxel only steps the detector row. sinop is the padded copy
-// made by bp_bilinear_prep_kernel, so no read needs a bounds test once its
-// indices are clamped into the padding (positions outside the detector read
-// zeros, as bilinear interpolation with a zero border does).
-template <int kRun>
+// part), then per voxel only steps the detector row and reads one quad.
+// sinoq is the quad copy made by bp_bilinear_prep_kernel, so no read needs a
+// bounds test once its indices are clamped into the padding (positions
+// outside the detector read zeros, as bilinear interpolation with a zero
+// border does); a z-run whose rows all lie inside skips the row clamps.
+template <int kRun, bool kCone>
 __global__ void __launch_bounds__(kBpX* kBpY)
     bp_bilinear_z_kernel(const AngleParams* __restrict__ params, const int* __restrict__ angles,
-                         int n_angles, const float* __restrict__ sinop, float* __restrict__ vol,
+                         int n_angles, const float4* __restrict__ sinoq, float* __restrict__ vol,
                          DeviceGeometry g, int additive) {
   const int x = blockIdx.x * kBpX + threadIdx.x;
   const int y = blockIdx.y * kBpY + threadIdx.y;
   const int z0 = blockIdx.z * kRun;
   if (x >= g.nx || y >= g.ny) return;
-  const bool cone = g.kind == TSGB_CONE;
   const float xt = float(x - g.ox), yt = float(y - g.oy), zt0 = float(z0 - g.oz);
   const int cp = g.cols + 2 * kColPad;
-  const int rs = g.nangles * cp;  // padded row stride (padded copy < 2^31 floats)
-  const float* __restrict__ base0 = sinop + kRowPad * rs + kColPad;
+  const int rs = g.nangles * cp;  // padded row stride (padded copy < 2^31 quads)
+  const float4* __restrict__ base0 = sinoq + kRowPad * rs + kColPad;
   const float umin = float(-kColPad - g.ou), umax = float(g.cols - g.ou);
   const float vmin = float(-kRowPad - g.ov), vmax = float(g.rows - g.ov);
   float acc[kRun];
@@ -415,28 +428,36 @@ __global__ void __launch_bounds__(kBpX* kBpY)
     const float ut = fmaf(ap.pu[1], yt, fmaf(ap.pu[2], xt, ap.pu[3])) * inw;
     const float fu0 = floorf(ut);
     const float fu = ut - fu0;
-    const float* __restrict__ colp = base0 + theta * cp + ((int)fminf(fmaxf(fu0, umin), umax) + g.ou);
-    const float nvc = fmaf(ap.pv[1], yt, fmaf(ap.pv[2], xt, ap.pv[3]));
-    float K = ap.bil_scale, dxy2 = 0.0f;
-    if (cone) {
+    // this column's quads, row 0 (anchored rows count from -ov)
+    const float4* __restrict__ colq =
+        base0 + theta * cp + ((int)fminf(fmaxf(fu0, umin), umax) + g.ou) + g.ov * rs;
+    // vt(j) = (pv0 (zt0 + j) + pv . [y, x, 1]) / w, linear in j
+    const float vt0 = fmaf(ap.pv[0], zt0, fmaf(ap.pv[1], yt, fmaf(ap.pv[2], xt, ap.pv[3]))) * inw;
+    const float dv = ap.pv[0] * inw;
+    float K = ap.bil_scale, dxy2 = 0.0f, dz0 = 0.0f;
+    if (kCone) {
       K *= inw * inw * inw;
       const float dx = (xt - ap.src[2]) * g.vs[2], dy = (yt - ap.src[1]) * g.vs[1];
       dxy2 = fmaf(dx, dx, dy * dy);
+      dz0 = (zt0 - ap.src[0]) * g.vs[0];
     }
+    const float vt1 = fmaf(float(kRun - 1), dv, vt0);
+    // vt is monotone in j: if both ends read rows inside [vmin, vmax] so does
+    // every voxel (NaN fails the test and takes the clamped loop).
+    const bool inside = fminf(vt0, vt1) >= vmin && fmaxf(vt0, vt1) < vmax + 1.0f;
 #pragma unroll
     for (int j = 0; j < kRun; ++j) {
-      const float zt = zt0 + float(j);
-      const float vt = fmaf(ap.pv[0], zt, nvc) * inw;
-      const float fv0 = floorf(vt);
+      const float vt = fmaf(float(j), dv, vt0);
+      float fv0 = floorf(vt);
       const float fv = vt - fv0;
-      const float* p = colp + ((int)fminf(fmaxf(fv0, vmin), vmax) + g.ov) * rs;
-      const float v00 = __ldg(p), v01 = __ldg(p + 1), v10 = __ldg(p + rs), v11 = __ldg(p + rs + 1);
-      const float top = fmaf(fu, v01 - v00, v00);
-      const float bot = fmaf(fu, v11 - v10, v10);
+      if (!inside) fv0 = fminf(fmaxf(fv0, vmin), vmax);  // rows outside read the zero padding
+      const float4 q = __ldg(colq + (int)fv0 * rs);
+      const float top = fmaf(fu, q.y - q.x, q.x);
+      const float bot = fmaf(fu, q.w - q.z, q.z);
       const float val = fmaf(fv, bot - top, top);
       float c = K;
-      if (cone) {
-        const float dz = (zt - ap.src[0]) * g.vs[0];
+      if (kCone) {
+        const float dz = fmaf(float(j), g.vs[0], dz0);
         const float l2 = fmaf(dz, dz, dxy2);
         c *= l2 * rsqrtf(l2);
       }
@@ -532,12 +553,16 @@ int launch_bp_bilinear(const tsgb_projector* p, float* vol, const float* sino, b
   if (p->n_bil_fast > 0) {
     const long long total = (long long)(g.rows + 2 * kRowPad) * g.nangles * (g.cols + 2 * kColPad);
     const long long blocks = (total + 255) / 256;
+    float4* quads = reinterpret_cast<float4*>(workspace);
     bp_bilinear_prep_kernel<<<int(blocks < 152LL * 64 ? blocks : 152LL * 64), 256, 0, stream>>>(
-        sino, workspace, g);
+        sino, quads, g);
     const dim3 grid((g.nx + kBpX - 1) / kBpX, (g.ny + kBpY - 1) / kBpY, (g.nz + kRunZ - 1) / kRunZ);
-    bp_bilinear_z_kernel<kRunZ><<<grid, block, 0, stream>>>(p->d_params, p->d_bil_fast,
-                                                            p->n_bil_fast, workspace, vol, g,
-                                                            additive ? 1 : 0);
+    if (g.kind == TSGB_CONE)
+      bp_bilinear_z_kernel<kRunZ, true><<<grid, block, 0, stream>>>(
+          p->d_params, p->d_bil_fast, p->n_bil_fast, quads, vol, g, additive ? 1 : 0);
+    else
+      bp_bilinear_z_kernel<kRunZ, false><<<grid, block, 0, stream>>>(
+          p->d_params, p->d_bil_fast, p->n_bil_fast, quads, vol, g, additive ? 1 : 0);
     written = true;
   }
   if (p->n_bil_slow > 0 || !written) {

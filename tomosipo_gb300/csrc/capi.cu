@@ -130,8 +130,9 @@ int64_t tsgb_fp_workspace_bytes(const tsgb_projector* p) {
 int64_t tsgb_bp_workspace_bytes(const tsgb_projector* p, int32_t bp_kind) {
   if (!p) return fail(TSGB_ERR_INVALID, "projector is NULL");
   if (bp_kind == TSGB_BP_BILINEAR)
+    // quad copy of the padded sinogram: four floats per element
     return p->n_bil_fast > 0 ? int64_t(p->g.rows + 2 * tsgb::kRowPad) * p->g.nangles *
-                                   (p->g.cols + 2 * tsgb::kColPad) * int64_t(sizeof(float))
+                                   (p->g.cols + 2 * tsgb::kColPad) * int64_t(4 * sizeof(float))
                              : 0;
   if (bp_kind != TSGB_BP_MATCHED) return fail(TSGB_ERR_INVALID, "unknown bp_kind");
   // row-pair weighted sinogram: two floats per pixel, kRowPad padding rows
