@@ -95,6 +95,14 @@ def test_batched_rejects_tilted_detectors(dev):
         BatchedSirt([(A, y)])
 
 
+def test_batched_rejects_detector_supersampling(dev):
+    vg = ts.volume(shape=16, size=1)
+    A = ts.operator(vg, ts.cone(angles=8, shape=(16, 24), size=1.5, cone_angle=0.4),
+                    detector_supersampling=2)
+    with pytest.raises(RuntimeError, match="supersampling"):
+        BatchedSirt([(A, torch.zeros(A.range_shape, device=dev))])
+
+
 def test_server_results_same_alone_and_in_mix(dev):
     """Continuous batching: jobs arriving over time, different sizes; each result
     equals the same request run alone (and the plain SIRT loop)."""

@@ -85,6 +85,10 @@ int tsgb_sirt_batch_create(const tsgb_sirt_job* jobs, int32_t n_jobs, tsgb_sirt_
       return bfail(TSGB_ERR_INVALID, "job " + std::to_string(i) +
                                          " has angles outside the separable backprojector "
                                          "(det_v not along z); run it with the plain operator");
+    if (p->fine)
+      return bfail(TSGB_ERR_INVALID, "job " + std::to_string(i) +
+                                         " uses detector supersampling; run it with the plain "
+                                         "operator");
     const tsgb::DeviceGeometry& g = p->g;
     work[i] = double(g.nz) * g.ny * g.nx * g.nangles;
   }

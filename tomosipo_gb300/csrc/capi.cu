@@ -71,12 +71,14 @@ int tsgb_projector_create(const tsgb_volume_desc* vol, const tsgb_projection_des
   g_last_error.clear();
   if (!out) return fail(TSGB_ERR_INVALID, "out is NULL");
   *out = nullptr;
+  if (detector_supersampling < 1 || detector_supersampling > 16)
+    return fail(TSGB_ERR_INVALID, "supersampling factors must lie in [1, 16]");
   tsgb_projector* p = new (std::nothrow) tsgb_projector();
   if (!p) return fail(TSGB_ERR_INVALID, "host allocation failed");
   std::vector<tsgb::ColumnEntry> columns;
   std::vector<int> sep, gen, bfast, bslow;
-  std::string err = tsgb::build_plan(vol, proj, voxel_supersampling, detector_supersampling, p,
-                                     &columns, &sep, &gen, &bfast, &bslow);
+  std::string err = tsgb::build_plan(vol, proj, voxel_supersampling, 1, p, &columns, &sep, &gen,
+                                     &bfast, &bslow);
   if (!err.empty()) {
     delete p;
     return fail(TSGB_ERR_INVALID, err);
@@ -94,6 +96,24 @@ int tsgb_projector_create(const tsgb_volume_desc* vol, const tsgb_projection_des
                 "<= 262140 and columns <= 524280");
   }
   p->tuning = tsgb::default_tuning(p);
+  if (detector_supersampling > 1) {
+    // the d-times finer detector: same centre, pixel vectors divided by d
+    const int d = detector_supersampling;
+    std::vector<double> fine(size_t(proj->num_angles) * 12);
+    for (size_t i = 0; i < fine.size(); ++i)
+      fine[i] = proj->vectors[i] / ((i % 12) >= 6 ? double(d) : 1.0);
+    tsgb_projection_desc fd = *proj;
+    fd.det_shape[0] = proj->det_shape[0] * d;
+    fd.det_shape[1] = proj->det_shape[1] * d;
+    fd.vectors = fine.data();
+    int rc = tsgb_projector_create(vol, &fd, voxel_supersampling, 1, &p->fine);
+    if (rc != TSGB_OK) {
+      delete p;
+      return fail(rc, "supersampled detector: " + g_last_error);
+    }
+    p->det_ss = d;
+    p->g.det_ss = d;
+  }
   cudaError_t e = cudaGetDevice(&p->device);
   if (e == cudaSuccess) e = upload(&p->d_params, p->host_params);
   if (e == cudaSuccess) e = upload(&p->d_columns, columns);
@@ -103,6 +123,7 @@ int tsgb_projector_create(const tsgb_volume_desc* vol, const tsgb_projection_des
   if (e == cudaSuccess) e = upload(&p->d_bil_slow, bslow);
   if (e != cudaSuccess) {
     free_device(p);
+    if (p->fine) tsgb_projector_destroy(p->fine);
     delete p;
     return cuda_fail(e, "projector upload");
   }
@@ -118,12 +139,25 @@ int tsgb_projector_destroy(tsgb_projector* p) {
   if (prev != p->device) cudaSetDevice(p->device);
   free_device(p);
   if (prev >= 0 && prev != p->device) cudaSetDevice(prev);
+  if (p->fine) tsgb_projector_destroy(p->fine);
   delete p;
   return TSGB_OK;
 }
 
+namespace {
+
+// Bytes of p->fine's sinogram, rounded up to 256 (the workspace part that
+// precedes p->fine's own workspace when the detector is supersampled).
+int64_t fine_sino_bytes(const tsgb_projector* p) {
+  const tsgb::DeviceGeometry& f = p->fine->g;
+  return (int64_t(f.rows) * f.nangles * f.cols * int64_t(sizeof(float)) + 255) / 256 * 256;
+}
+
+}  // namespace
+
 int64_t tsgb_fp_workspace_bytes(const tsgb_projector* p) {
   if (!p) return fail(TSGB_ERR_INVALID, "projector is NULL");
+  if (p->fine) return fine_sino_bytes(p) + tsgb_fp_workspace_bytes(p->fine);
   return p->fp_workspace_elems * int64_t(2 * sizeof(float));  // pairs of floats
 }
 
@@ -135,6 +169,7 @@ int64_t tsgb_bp_workspace_bytes(const tsgb_projector* p, int32_t bp_kind) {
                                    (p->g.cols + 2 * tsgb::kColPad) * int64_t(4 * sizeof(float))
                              : 0;
   if (bp_kind != TSGB_BP_MATCHED) return fail(TSGB_ERR_INVALID, "unknown bp_kind");
+  if (p->fine) return fine_sino_bytes(p) + tsgb_bp_workspace_bytes(p->fine, bp_kind);
   // row-pair weighted sinogram: two floats per pixel, kRowPad padding rows
   return int64_t(p->g.rows + 2 * tsgb::kRowPad) * p->g.nangles * p->g.cols * int64_t(2 * sizeof(float));
 }
@@ -164,8 +199,17 @@ int tsgb_direct_fp(tsgb_projector* p, const float* vol, float* sino, int32_t add
                                         " bytes of workspace");
   int rc = check_device(p);
   if (rc != TSGB_OK) return rc;
-  cudaError_t e = cudaError_t(
-      tsgb::launch_fp(p, vol, sino, additive != 0, static_cast<float*>(workspace), stream));
+  cudaError_t e;
+  if (p->fine) {
+    // project onto the finer detector, then bin d x d blocks into sino
+    float* fine_sino = static_cast<float*>(workspace);
+    float* fine_ws = reinterpret_cast<float*>(static_cast<char*>(workspace) + fine_sino_bytes(p));
+    e = cudaError_t(tsgb::launch_fp(p->fine, vol, fine_sino, false, fine_ws, stream));
+    if (e == cudaSuccess) e = cudaError_t(tsgb::launch_ss_bin(p, fine_sino, sino, additive != 0, stream));
+  } else {
+    e = cudaError_t(
+        tsgb::launch_fp(p, vol, sino, additive != 0, static_cast<float*>(workspace), stream));
+  }
   if (e != cudaSuccess) return cuda_fail(e, "forward projection launch");
   return TSGB_OK;
 }
@@ -183,7 +227,15 @@ int tsgb_direct_bp(tsgb_projector* p, float* vol, const float* sino, int32_t add
   int rc = check_device(p);
   if (rc != TSGB_OK) return rc;
   cudaError_t e;
-  if (bp_kind == TSGB_BP_MATCHED)
+  if (bp_kind == TSGB_BP_MATCHED && p->fine) {
+    // the transpose of the binning: spread each pixel / d^2 over its block,
+    // then the finer detector's matched backprojection
+    float* fine_sino = static_cast<float*>(workspace);
+    float* fine_ws = reinterpret_cast<float*>(static_cast<char*>(workspace) + fine_sino_bytes(p));
+    e = cudaError_t(tsgb::launch_ss_expand(p, sino, fine_sino, stream));
+    if (e == cudaSuccess)
+      e = cudaError_t(tsgb::launch_bp_matched(p->fine, vol, fine_sino, additive != 0, fine_ws, stream));
+  } else if (bp_kind == TSGB_BP_MATCHED)
     e = cudaError_t(tsgb::launch_bp_matched(p, vol, sino, additive != 0,
                                             static_cast<float*>(workspace), stream));
   else
@@ -195,14 +247,19 @@ int tsgb_direct_bp(tsgb_projector* p, float* vol, const float* sino, int32_t add
 
 int tsgb_projector_stats(const tsgb_projector* p, int64_t* out, int32_t n) {
   if (!p || !out || n < 0 || n > 8) return fail(TSGB_ERR_INVALID, "bad stats arguments");
-  const int64_t chunks = (p->g.nangles + 65534) / 65535;
-  const int64_t chunk = tsgb::fp_angle_chunk(p->g);
-  const int64_t fp_launches = int64_t(p->layouts.size()) + (p->g.nangles + chunk - 1) / chunk;
-  const int64_t bp_launches =
-      chunks + (p->n_separable_bp > 0 ? 1 : 0) + ((p->n_general_bp > 0 || p->n_separable_bp == 0) ? 1 : 0);
-  const int64_t vals[8] = {int64_t(p->layouts.size()),
-                           p->n_separable_bp,
-                           p->n_general_bp,
+  // FP and matched BP run on the finer detector when it is supersampled, plus
+  // one binning / spreading launch
+  const tsgb_projector* f = p->fine ? p->fine : p;
+  const int64_t extra = p->fine ? 1 : 0;
+  const int64_t chunks = (f->g.nangles + 65534) / 65535;
+  const int64_t chunk = tsgb::fp_angle_chunk(f->g);
+  const int64_t fp_launches =
+      int64_t(f->layouts.size()) + (f->g.nangles + chunk - 1) / chunk + extra;
+  const int64_t bp_launches = chunks + (f->n_separable_bp > 0 ? 1 : 0) +
+                              ((f->n_general_bp > 0 || f->n_separable_bp == 0) ? 1 : 0) + extra;
+  const int64_t vals[8] = {int64_t(f->layouts.size()),
+                           f->n_separable_bp,
+                           f->n_general_bp,
                            fp_launches,
                            bp_launches,
                            (p->n_bil_fast > 0 ? 2 : 0) +
@@ -216,7 +273,7 @@ int tsgb_projector_stats(const tsgb_projector* p, int64_t* out, int32_t n) {
 int tsgb_projector_get_tuning(const tsgb_projector* p, tsgb_tuning* out) {
   g_last_error.clear();
   if (!p || !out) return fail(TSGB_ERR_INVALID, "projector or out is NULL");
-  *out = p->tuning;
+  *out = p->fine ? p->fine->tuning : p->tuning;  // the projector that runs the FP
   return TSGB_OK;
 }
 
@@ -229,7 +286,7 @@ int tsgb_projector_set_tuning(tsgb_projector* p, const tsgb_tuning* t) {
     return fail(TSGB_ERR_INVALID, "fp_pair_layout must be 0 or 1");
   for (int i = 0; i < 4; ++i)
     if (t->reserved[i] != 0) return fail(TSGB_ERR_INVALID, "reserved tuning fields must be 0");
-  p->tuning = *t;
+  (p->fine ? p->fine : p)->tuning = *t;  // the projector that runs the FP
   return TSGB_OK;
 }
 

@@ -59,7 +59,7 @@ std::string build_plan(const tsgb_volume_desc* vol, const tsgb_projection_desc* 
     return "projection kind must be TSGB_PARALLEL or TSGB_CONE";
   if (voxel_ss < 1 || det_ss < 1 || voxel_ss > 16 || det_ss > 16)
     return "supersampling factors must lie in [1, 16]";
-  if (det_ss != 1) return "detector supersampling > 1 is not implemented on the GPU yet";
+  if (det_ss != 1) return "the plan is built per detector; supersampling is a finer detector";
   for (int i = 0; i < 3; ++i) {
     if (vol->shape[i] < 1 || vol->shape[i] > (1 << 20)) return "volume shape out of range";
     if (!(vol->size[i] > 0) || !std::isfinite(vol->size[i]) || !std::isfinite(vol->pos[i]))

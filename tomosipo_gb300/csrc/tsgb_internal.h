@@ -107,6 +107,12 @@ struct tsgb_projector {
   int device;
   tsgb::DeviceGeometry g;
   tsgb_tuning tuning;
+  // Detector supersampling d > 1: `fine` projects onto the d-times finer
+  // detector (forward projection and matched backprojection run there, with
+  // binning / spreading passes; supersample.cu); this projector keeps the
+  // coarse detector for shapes and the bilinear backprojection.
+  int det_ss = 1;
+  tsgb_projector* fine = nullptr;
   std::vector<tsgb::AngleParams> host_params;
   std::vector<tsgb::Layout> layouts;
   int64_t fp_workspace_elems = 0;  // 8-byte pair elements
@@ -139,6 +145,11 @@ FpSchedule fp_schedule(const tsgb_projector* p, int pairs);
 long long fp_angle_chunk(const DeviceGeometry& g);
 // Default tuning of a new projector whose plan is built (fp.cu).
 tsgb_tuning default_tuning(const tsgb_projector* p);
+
+// Detector supersampling passes between p's detector and p->fine's (supersample.cu).
+int launch_ss_bin(const tsgb_projector* p, const float* fine, float* coarse, bool additive,
+                  void* stream);
+int launch_ss_expand(const tsgb_projector* p, const float* coarse, float* fine, void* stream);
 
 // Sets the calling thread's message returned by tsgb_last_error (capi.cu).
 void set_last_error(const std::string& msg);
