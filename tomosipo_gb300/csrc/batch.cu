@@ -139,7 +139,10 @@ int tsgb_sirt_batch_iterate(tsgb_sirt_batch* b, int32_t iterations, void* stream
       cudaStream_t s = b->streams[i % K];
       const tsgb::FpSirt sirt{J.sino, J.R, J.residual};
       e = cudaError_t(tsgb::launch_fp(J.projector, J.vol, nullptr, false, J.fp_workspace, s, &sirt));
-      if (e == cudaSuccess) e = cudaError_t(tsgb::launch_bp_sirt(J.projector, J.vol, J.C, J.residual, s));
+      // the forward workspace is free once the residual is written: it holds
+      // the first backprojection pass's sum
+      if (e == cudaSuccess)
+        e = cudaError_t(tsgb::launch_bp_sirt(J.projector, J.vol, J.C, J.residual, J.fp_workspace, s));
     }
   }
   for (int k = 0; k < K && e == cudaSuccess; ++k) {

@@ -71,40 +71,50 @@ __global__ void __launch_bounds__(256)
   out[((long long)iv * g.nangles + theta) * g.cols + iu] = make_float2(a, b);
 }
 
-// Matched backprojection of the angles in `angles` for the voxel column
-// (x, y) and the kRun voxels z0 .. z0 + kRun - 1, accumulated into acc.
+// Matched backprojection of separable angles (det_v along z, so b = z) that
+// share their in-plane axis a, for kA voxel columns adjacent along a (at
+// a-coordinates it0 .. it0 + kA - 1, all on the plane kt of the dominant axis
+// d) and the kRun voxels z0 .. z0 + kRun - 1, accumulated into acc.
+//
+// A detector column iu reaches the voxels of plane kt through
+//   h = tent(q_a(iu, kt) - it)           (in-plane weight, one per voxel)
+//   V(z) = sum_v tent(q_b(iu, v, kt) - z) W y[v][iu]   (vertical profile)
+// and V does not depend on it, so the kA voxels share it: per column and z
+// the profile is built once and added with each voxel's h. The columns
+// visited are those whose ray passes plane kt within one voxel of any of the
+// kA voxels: solve (A0 + A1 u) / (e0 + e1 u) = it0 - 1 and it0 + kA for u.
+//
 // sinow is the row-pair weighted sinogram (bp_weight_kernel) with kRowPad
 // padding rows above and below the detector (rows -kRowPad .. rows + kRowPad
 // - 1), so the two-row path reads both rows with one load and without bounds
 // tests once its row index is clamped into the padding. Offsets (in pairs)
 // are 32-bit unless kWide (padded sinogram of 2^31 pairs or more).
-template <int kRun, bool kWide>
-__device__ __forceinline__ void bp_separable_accumulate(
-    const AngleParams* __restrict__ params, const ColumnEntry* __restrict__ columns,
-    const int* __restrict__ angles, int n_angles, const float2* __restrict__ sinow,
-    const DeviceGeometry& g, int x, int y, int z0, float (&acc)[kRun]) {
+template <int kA, int kRun, bool kWide>
+__device__ __forceinline__ void bp_sep_accumulate(const AngleParams* __restrict__ params,
+                                                  const ColumnEntry* __restrict__ columns,
+                                                  const int* __restrict__ angles, int n_angles,
+                                                  const float2* __restrict__ sinow,
+                                                  const DeviceGeometry& g, float kt, float it0,
+                                                  int z0, float (&acc)[kA][kRun]) {
   using Offset = typename std::conditional<kWide, long long, int>::type;
-  const float xt = float(x - g.ox), yt = float(y - g.oy);
   const float zt0 = float(z0 - g.oz);
   const Offset rs = Offset(g.nangles) * g.cols;  // row stride
   const float2* __restrict__ sinow0 = sinow + (long long)kRowPad * rs;  // row 0
   const float vmin = float(-kRowPad - g.ov), vmax = float(g.rows - g.ov);
   const float4* __restrict__ col4 = reinterpret_cast<const float4*>(columns);
 #pragma unroll
-  for (int j = 0; j < kRun; ++j) acc[j] = 0.0f;
+  for (int m = 0; m < kA; ++m)
+#pragma unroll
+    for (int j = 0; j < kRun; ++j) acc[m][j] = 0.0f;
 
   for (int n = 0; n < n_angles; ++n) {
     const int theta = __ldg(angles + n);
     const AngleParams& ap = params[theta];
-    // b = z here, so (d, a) is (x, y) or (y, x).
-    const float kt = ap.d == 2 ? xt : yt;
-    const float it = ap.d == 2 ? yt : xt;
-    // Columns whose rays pass plane kt within one voxel of it: solve
-    // (A0 + A1 u) / (e0 + e1 u) = it -+ 1 for u. Only the range needs this;
-    // the weights below are exact, so fast division is enough.
+    // Only the range needs this solve; the weights below are exact, so fast
+    // division is enough.
     const float A0 = fmaf(kt, ap.ma[0], ap.ca[0]);
     const float A1 = fmaf(kt, ap.ma[1], ap.ca[1]);
-    const float tl = it - 1.0f, th = it + 1.0f;
+    const float tl = it0 - 1.0f, th = it0 + float(kA);
     const float u1 = __fdividef(fmaf(tl, ap.e[0], -A0), fmaf(-tl, ap.e[1], A1));
     const float u2 = __fdividef(fmaf(th, ap.e[0], -A0), fmaf(-th, ap.e[1], A1));
     const int iu_lo = max(0, (int)floorf(clamp_coord(fminf(u1, u2))) + 1 + g.ou);
@@ -114,8 +124,15 @@ __device__ __forceinline__ void bp_separable_accumulate(
       const size_t ci = ((size_t)theta * g.cols + iu) * 2;
       const float4 c0 = __ldg(col4 + ci);      // Xa, ma, P, Q
       const float4 c1 = __ldg(col4 + ci + 1);  // R, S, -, -
-      const float h = 1.0f - fabsf(fmaf(kt, c0.y, c0.x) - it);
-      if (h <= 0.0f) continue;
+      const float qa = fmaf(kt, c0.y, c0.x) - it0;
+      float h[kA];
+      bool any = false;
+#pragma unroll
+      for (int m = 0; m < kA; ++m) {
+        h[m] = fmaxf(0.0f, 1.0f - fabsf(qa - float(m)));
+        any = any || h[m] > 0.0f;
+      }
+      if (!any) continue;
       // On plane kt, q_b(vt) = B + vt * Sl.
       const float B = fmaf(kt, c0.w, c0.z);
       const float Sl = fmaf(kt, c1.y, c1.x);
@@ -126,39 +143,26 @@ __device__ __forceinline__ void bp_separable_accumulate(
         // Voxel j's row position vs = (z_j - B) / Sl; row v0's ray passes the
         // plane at t0 = q_b - z_j = v0 Sl + (B - zt0) - j = -Sl (vs - v0), and
         // row v0+1's at t0 + Sl, so |t0 + Sl| = |Sl| - |t0| for the rows the
-        // run selects. The column weight h is folded into the tents:
-        //   h tent(t0) = max(0, h - h |t0|),
-        //   h tent(t0 + Sl) = max(0, h (1 - |Sl|) + h |t0|).
+        // run selects: tent(t0 + Sl) = max(0, 1 - |Sl| + |t0|).
         const float vs0 = (zt0 - B) * inv;
         const float vs1 = fmaf(float(kRun - 1), inv, vs0);
         const float C0 = B - zt0;
-        const float nh = -h;
-        const float h1 = h - h * fabsf(Sl);
+        const float c1s = 1.0f - fabsf(Sl);
         const float2* __restrict__ colv = col + Offset(g.ov) * rs;  // row 0 of this column
         // vs is monotone in j: if both ends select rows inside [vmin, vmax]
         // every voxel does, and no clamping is needed (NaN fails the test).
-        if (fminf(vs0, vs1) >= vmin && fmaxf(vs0, vs1) < vmax + 1.0f) {
+        const bool inside = fminf(vs0, vs1) >= vmin && fmaxf(vs0, vs1) < vmax + 1.0f;
 #pragma unroll
-          for (int j = 0; j < kRun; ++j) {
-            const float v0 = floorf(fmaf(float(j), inv, vs0));
-            const float t0 = fmaf(v0, Sl, C0) - float(j);
-            const float2 yy = __ldg(colv + Offset((int)v0) * rs);
-            const float at0 = fabsf(t0);
-            acc[j] = fmaf(fmaxf(0.0f, fmaf(nh, at0, h)), yy.x,
-                          fmaf(fmaxf(0.0f, fmaf(h, at0, h1)), yy.y, acc[j]));
-          }
-        } else {
+        for (int j = 0; j < kRun; ++j) {
+          float v0 = floorf(fmaf(float(j), inv, vs0));
+          // Rows outside [-kRowPad, rows] hold zeros either way: clamping
+          // keeps both reads inside the padding (NaN clamps to the low end).
+          if (!inside) v0 = fminf(fmaxf(v0, vmin), vmax);
+          const float at0 = fabsf(fmaf(v0, Sl, C0) - float(j));
+          const float2 yy = __ldg(colv + Offset((int)v0) * rs);
+          const float V = fmaf(fmaxf(0.0f, 1.0f - at0), yy.x, fmaxf(0.0f, c1s + at0) * yy.y);
 #pragma unroll
-          for (int j = 0; j < kRun; ++j) {
-            // Rows outside [-kRowPad, rows] hold zeros either way: clamping
-            // keeps both reads inside the padding (NaN clamps to the low end).
-            const float v0 = fminf(fmaxf(floorf(fmaf(float(j), inv, vs0)), vmin), vmax);
-            const float t0 = fmaf(v0, Sl, C0) - float(j);
-            const float2 yy = __ldg(colv + Offset((int)v0) * rs);
-            const float at0 = fabsf(t0);
-            acc[j] = fmaf(fmaxf(0.0f, fmaf(nh, at0, h)), yy.x,
-                          fmaf(fmaxf(0.0f, fmaf(h, at0, h1)), yy.y, acc[j]));
-          }
+          for (int m = 0; m < kA; ++m) acc[m][j] = fmaf(h[m], V, acc[m][j]);
         }
       } else {
 #pragma unroll
@@ -167,44 +171,73 @@ __device__ __forceinline__ void bp_separable_accumulate(
           const float v1 = (-1.0f - Bj) * inv, v2 = (1.0f - Bj) * inv;
           const int iv_lo = max(0, (int)floorf(clamp_coord(fminf(v1, v2))) + g.ov);
           const int iv_hi = min(g.rows - 1, (int)ceilf(clamp_coord(fmaxf(v1, v2))) + g.ov);
-          float s = 0.0f;
+          float V = 0.0f;
           for (int iv = iv_lo; iv <= iv_hi; ++iv) {
             const float w = tent(fmaf(float(iv - g.ov), Sl, Bj));
-            s = fmaf(w, __ldg(col + Offset(iv) * rs).x, s);
+            V = fmaf(w, __ldg(col + Offset(iv) * rs).x, V);
           }
-          acc[j] = fmaf(h, s, acc[j]);
+#pragma unroll
+          for (int m = 0; m < kA; ++m) acc[m][j] = fmaf(h[m], V, acc[m][j]);
         }
       }
     }
   }
 }
 
-// One thread per (x, y) voxel column and run of kRun voxels along z.
-// kSirt: SIRT update x += C * A^T(res) instead of writing the backprojection,
-// rounded as the plain recipe's x += C * bp (C is then the per-voxel weight).
-template <int kRun, bool kWide, bool kSirt>
-__global__ void __launch_bounds__(kBpX* kBpY)
+// Epilogues of bp_separable_kernel.
+enum BpSepMode {
+  kBpSet = 0,        // vol = A^T y
+  kBpAdd = 1,        // vol += A^T y
+  kBpSirtFirst = 2,  // scratch = this pass's sum (the first of two SIRT passes)
+  kBpSirtLast = 3,   // vol += C * (scratch + this pass's sum), or C * sum alone
+};
+
+// One pass of the matched backprojection over the separable angles whose
+// in-plane axis is x (kAisX: each thread owns kA voxel columns adjacent along
+// x on one y) or y (kA columns adjacent along y on one x), with kRun voxels
+// along z. The two passes together cover all separable angles; the second
+// adds onto the first. In SIRT mode the first pass's sum waits in `scratch`
+// so the update x += C * (sum1 + sum2) rounds as the plain recipe's
+// vol = sum1; vol += sum2; x += C * vol. Six resident blocks per SM (80
+// registers) measured fastest for 2 x 16 voxels per thread: fewer registers
+// spill the accumulators, more cut occupancy.
+template <int kA, int kRun, bool kWide, bool kAisX, int kMode>
+__global__ void __launch_bounds__(kBpX* kBpY, 6)
     bp_separable_kernel(const AngleParams* __restrict__ params,
                         const ColumnEntry* __restrict__ columns, const int* __restrict__ angles,
                         int n_angles, const float2* __restrict__ sinow, float* __restrict__ vol,
-                        DeviceGeometry g, int additive, const float* __restrict__ C) {
-  const int x = blockIdx.x * kBpX + threadIdx.x;
-  const int y = blockIdx.y * kBpY + threadIdx.y;
+                        DeviceGeometry g, const float* __restrict__ C,
+                        float* __restrict__ scratch) {
+  const int x0 = (blockIdx.x * kBpX + threadIdx.x) * (kAisX ? kA : 1);
+  const int y0 = (blockIdx.y * kBpY + threadIdx.y) * (kAisX ? 1 : kA);
   const int z0 = blockIdx.z * kRun;
-  if (x >= g.nx || y >= g.ny) return;
-  float acc[kRun];
-  bp_separable_accumulate<kRun, kWide>(params, columns, angles, n_angles, sinow, g, x, y, z0, acc);
+  if (x0 >= g.nx || y0 >= g.ny) return;
+  const float xt = float(x0 - g.ox), yt = float(y0 - g.oy);
+  // a = x: the dominant axis is y (kt = y); a = y: it is x.
+  const float kt = kAisX ? yt : xt;
+  const float it0 = kAisX ? xt : yt;
+  float acc[kA][kRun];
+  bp_sep_accumulate<kA, kRun, kWide>(params, columns, angles, n_angles, sinow, g, kt, it0, z0,
+                                     acc);
 #pragma unroll
-  for (int j = 0; j < kRun; ++j) {
-    const int z = z0 + j;
-    if (z < g.nz) {
+  for (int m = 0; m < kA; ++m) {
+    const int x = kAisX ? x0 + m : x0, y = kAisX ? y0 : y0 + m;
+    if (x >= g.nx || y >= g.ny) continue;
+#pragma unroll
+    for (int j = 0; j < kRun; ++j) {
+      const int z = z0 + j;
+      if (z >= g.nz) continue;
       const size_t idx = ((size_t)z * g.ny + y) * g.nx + x;
-      if (kSirt)
-        vol[idx] = __fadd_rn(vol[idx], __fmul_rn(acc[j], __ldg(C + idx)));
-      else if (additive)
-        vol[idx] += acc[j];
-      else
-        vol[idx] = acc[j];
+      if (kMode == kBpSet) {
+        vol[idx] = acc[m][j];
+      } else if (kMode == kBpAdd) {
+        vol[idx] += acc[m][j];
+      } else if (kMode == kBpSirtFirst) {
+        scratch[idx] = acc[m][j];
+      } else {
+        const float s = scratch ? __fadd_rn(scratch[idx], acc[m][j]) : acc[m][j];
+        vol[idx] = __fadd_rn(vol[idx], __fmul_rn(s, __ldg(C + idx)));
+      }
     }
   }
 }
@@ -479,6 +512,48 @@ __global__ void __launch_bounds__(kBpX* kBpY)
 
 }  // namespace
 
+namespace {
+
+constexpr int kSepA = 2;  // voxel columns per thread along a (matched)
+
+template <bool kWide, bool kAisX, int kMode>
+void launch_sep_pass_t(const tsgb_projector* p, const float2* pairs, float* vol, const float* C,
+                       float* scratch, cudaStream_t stream) {
+  const DeviceGeometry& g = p->g;
+  const int* angles = p->d_sep_angles + (kAisX ? 0 : p->n_sep_ax);
+  const int n = kAisX ? p->n_sep_ax : p->n_separable_bp - p->n_sep_ax;
+  const int tx = kBpX * (kAisX ? kSepA : 1), ty = kBpY * (kAisX ? 1 : kSepA);
+  const dim3 grid((g.nx + tx - 1) / tx, (g.ny + ty - 1) / ty, (g.nz + kRunZ - 1) / kRunZ);
+  bp_separable_kernel<kSepA, kRunZ, kWide, kAisX, kMode><<<grid, dim3(kBpX, kBpY), 0, stream>>>(
+      p->d_params, p->d_columns, angles, n, pairs, vol, g, C, scratch);
+}
+
+template <bool kWide, bool kAisX>
+void launch_sep_pass_m(const tsgb_projector* p, int mode, const float2* pairs, float* vol,
+                       const float* C, float* scratch, cudaStream_t stream) {
+  switch (mode) {
+    case kBpSet: launch_sep_pass_t<kWide, kAisX, kBpSet>(p, pairs, vol, C, scratch, stream); break;
+    case kBpAdd: launch_sep_pass_t<kWide, kAisX, kBpAdd>(p, pairs, vol, C, scratch, stream); break;
+    case kBpSirtFirst:
+      launch_sep_pass_t<kWide, kAisX, kBpSirtFirst>(p, pairs, vol, C, scratch, stream);
+      break;
+    default: launch_sep_pass_t<kWide, kAisX, kBpSirtLast>(p, pairs, vol, C, scratch, stream);
+  }
+}
+
+// One pass of the separable matched backprojection (a = x or a = y angles).
+void launch_sep_pass(const tsgb_projector* p, bool a_is_x, int mode, const float2* pairs,
+                     float* vol, const float* C, float* scratch, cudaStream_t stream) {
+  const DeviceGeometry& g = p->g;
+  const bool wide = (size_t)(g.rows + 2 * kRowPad) * g.nangles * g.cols >= (size_t(1) << 31);
+  if (wide && a_is_x) launch_sep_pass_m<true, true>(p, mode, pairs, vol, C, scratch, stream);
+  else if (wide) launch_sep_pass_m<true, false>(p, mode, pairs, vol, C, scratch, stream);
+  else if (a_is_x) launch_sep_pass_m<false, true>(p, mode, pairs, vol, C, scratch, stream);
+  else launch_sep_pass_m<false, false>(p, mode, pairs, vol, C, scratch, stream);
+}
+
+}  // namespace
+
 int launch_bp_matched(const tsgb_projector* p, float* vol, const float* sino, bool additive,
                       float* workspace, void* stream_) {
   cudaStream_t stream = static_cast<cudaStream_t>(stream_);
@@ -500,21 +575,13 @@ int launch_bp_matched(const tsgb_projector* p, float* vol, const float* sino, bo
   // rows .. rows + kRowPad - 1
   cudaMemsetAsync(pairs, 0, (kRowPad - 1) * rs * sizeof(float2), stream);
   cudaMemsetAsync(pairs + (kRowPad + g.rows) * rs, 0, kRowPad * rs * sizeof(float2), stream);
-  bool written = false;
-  if (p->n_separable_bp > 0) {
-    const dim3 block(kBpX, kBpY);
-    const dim3 grid((g.nx + kBpX - 1) / kBpX, (g.ny + kBpY - 1) / kBpY, (g.nz + kRunZ - 1) / kRunZ);
-    const bool wide = (size_t)(g.rows + 2 * kRowPad) * g.nangles * g.cols >= (size_t(1) << 31);
-    if (wide)
-      bp_separable_kernel<kRunZ, true, false><<<grid, block, 0, stream>>>(
-          p->d_params, p->d_columns, p->d_sep_angles, p->n_separable_bp, pairs, vol, g,
-          additive ? 1 : 0, nullptr);
-    else
-      bp_separable_kernel<kRunZ, false, false><<<grid, block, 0, stream>>>(
-          p->d_params, p->d_columns, p->d_sep_angles, p->n_separable_bp, pairs, vol, g,
-          additive ? 1 : 0, nullptr);
-    written = true;
-  }
+  const int n_ax = p->n_sep_ax, n_ay = p->n_separable_bp - p->n_sep_ax;
+  if (n_ax > 0)
+    launch_sep_pass(p, true, additive ? kBpAdd : kBpSet, pairs, vol, nullptr, nullptr, stream);
+  if (n_ay > 0)
+    launch_sep_pass(p, false, (additive || n_ax > 0) ? kBpAdd : kBpSet, pairs, vol, nullptr,
+                    nullptr, stream);
+  const bool written = p->n_separable_bp > 0;
   if (p->n_general_bp > 0 || !written) {
     const dim3 block(32, 4);
     const dim3 grid((g.nx + 31) / 32, (g.ny + 3) / 4, g.nz);
@@ -526,23 +593,18 @@ int launch_bp_matched(const tsgb_projector* p, float* vol, const float* sino, bo
 }
 
 int launch_bp_sirt(const tsgb_projector* p, float* vol, const float* C, const float* res,
-                   void* stream_) {
+                   float* scratch, void* stream_) {
   cudaStream_t stream = static_cast<cudaStream_t>(stream_);
-  const DeviceGeometry& g = p->g;
-  if (p->n_separable_bp == 0) return int(cudaGetLastError());
   const float2* pairs = reinterpret_cast<const float2*>(res);
-  const dim3 block(kBpX, kBpY);
-  const dim3 grid((g.nx + kBpX - 1) / kBpX, (g.ny + kBpY - 1) / kBpY, (g.nz + kRunZ - 1) / kRunZ);
-  const bool wide = (size_t)(g.rows + 2 * kRowPad) * g.nangles * g.cols >= (size_t(1) << 31);
-  if (wide)
-    bp_separable_kernel<kRunZ, true, true><<<grid, block, 0, stream>>>(
-        p->d_params, p->d_columns, p->d_sep_angles, p->n_separable_bp, pairs, vol, g, 0, C);
-  else
-    bp_separable_kernel<kRunZ, false, true><<<grid, block, 0, stream>>>(
-        p->d_params, p->d_columns, p->d_sep_angles, p->n_separable_bp, pairs, vol, g, 0, C);
+  const int n_ax = p->n_sep_ax, n_ay = p->n_separable_bp - p->n_sep_ax;
+  if (n_ax > 0 && n_ay > 0) {
+    launch_sep_pass(p, true, kBpSirtFirst, pairs, vol, C, scratch, stream);
+    launch_sep_pass(p, false, kBpSirtLast, pairs, vol, C, scratch, stream);
+  } else if (n_ax > 0 || n_ay > 0) {
+    launch_sep_pass(p, n_ax > 0, kBpSirtLast, pairs, vol, C, nullptr, stream);
+  }
   return int(cudaGetLastError());
 }
-
 
 int launch_bp_bilinear(const tsgb_projector* p, float* vol, const float* sino, bool additive,
                        float* workspace, void* stream_) {

@@ -255,7 +255,8 @@ int tsgb_projector_stats(const tsgb_projector* p, int64_t* out, int32_t n) {
   const int64_t chunk = tsgb::fp_angle_chunk(f->g);
   const int64_t fp_launches =
       int64_t(f->layouts.size()) + (f->g.nangles + chunk - 1) / chunk + extra;
-  const int64_t bp_launches = chunks + (f->n_separable_bp > 0 ? 1 : 0) +
+  const int64_t bp_launches = chunks + (f->n_sep_ax > 0 ? 1 : 0) +
+                              (f->n_separable_bp - f->n_sep_ax > 0 ? 1 : 0) +
                               ((f->n_general_bp > 0 || f->n_separable_bp == 0) ? 1 : 0) + extra;
   const int64_t vals[8] = {int64_t(f->layouts.size()),
                            f->n_separable_bp,

@@ -5,6 +5,7 @@
 // the projection geometry. Everything here runs once per projector, in
 // double precision, and is rounded to fp32 only at the end so the kernels
 // start from correctly rounded coefficients.
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <string>
@@ -297,7 +298,13 @@ std::string build_plan(const tsgb_volume_desc* vol, const tsgb_projection_desc* 
   }
   p->fp_workspace_elems = off;
   p->n_general_bp = int(gen_angles->size());
+  // Separable angles grouped by their in-plane axis a (x first, then y): the
+  // backprojector runs one pass per group, each with voxel runs along a.
+  std::stable_partition(sep_angles->begin(), sep_angles->end(),
+                        [&](int t) { return p->host_params[t].a == 2; });
   p->n_separable_bp = int(sep_angles->size());
+  p->n_sep_ax = int(std::count_if(sep_angles->begin(), sep_angles->end(),
+                                  [&](int t) { return p->host_params[t].a == 2; }));
   p->n_bil_fast = int(bil_fast->size());
   p->n_bil_slow = int(bil_slow->size());
   return std::string();

@@ -118,6 +118,7 @@ struct tsgb_projector {
   int64_t fp_workspace_elems = 0;  // 8-byte pair elements
   int n_general_bp = 0;         // angles handled by the general BP kernel
   int n_separable_bp = 0;       // angles handled by the separable BP kernel
+  int n_sep_ax = 0;             // of those, the first n_sep_ax have a = x (the rest a = y)
   int n_bil_fast = 0;           // bilinear BP: angles for the z-flat kernel
   int n_bil_slow = 0;           // bilinear BP: angles for the general kernel
   tsgb::AngleParams* d_params = nullptr;
@@ -175,8 +176,9 @@ int launch_bp_bilinear(const tsgb_projector* p, float* vol, const float* sino, b
 
 // SIRT update x += C * A^T(res) from a residual written by launch_fp's SIRT
 // epilogue (separable angles only), rounded as the plain recipe's x += C * bp.
+// scratch: a volume-sized buffer (the forward workspace is free by then).
 int launch_bp_sirt(const tsgb_projector* p, float* vol, const float* C, const float* res,
-                   void* stream);
+                   float* scratch, void* stream);
 constexpr int kBpRunZ = 16;  // voxels along z per matched-backprojection thread
 constexpr int kBpTileX = 32, kBpTileY = 4, kFpTileRows = 32, kFpTileCols = 8;
 
