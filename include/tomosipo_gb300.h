@@ -168,6 +168,21 @@ typedef struct {
 int tsgb_projector_get_tuning(const tsgb_projector* p, tsgb_tuning* out);
 int tsgb_projector_set_tuning(tsgb_projector* p, const tsgb_tuning* t);
 
+/* FDK backprojection (the backprojection step of tomosipo's fdk,
+ * tomosipo/astra.py:374-406, which calls ASTRA's accumulate_FDK): for cone
+ * beams whose detector v axis runs along z (circular and helical scans),
+ *   vol (+)= sum_t angle_weights[t] * q_t(u_t(x), v_t(x)) / w_t(x)^2
+ * where q is the already weighted and ramp-filtered sinogram (layout as any
+ * sinogram), read with bilinear interpolation and zero outside the detector,
+ * and w_t(x) is the voxel's depth along the detector normal divided by the
+ * volume anchor's (the centre of voxel (nz/2, ny/2, nx/2)). angle_weights is a
+ * device array of num_angles floats. Workspace: tsgb_bp_workspace_bytes(p,
+ * TSGB_BP_BILINEAR). The weighting and filtering steps are the caller's
+ * (tomosipo_gb300/fdk.py). */
+int tsgb_fdk_backproject(tsgb_projector* p, float* vol, const float* filtered,
+                         const float* angle_weights, int32_t additive, void* workspace,
+                         int64_t workspace_bytes, void* stream);
+
 /* Shapes the projector expects: vol (z, y, x) and sino (rows, angles, cols). */
 int tsgb_projector_shapes(const tsgb_projector* p, int64_t vol_shape[3],
                           int64_t sino_shape[3]);

@@ -1,0 +1,79 @@
+"""FP64 NumPy FDK -- TEST INFRASTRUCTURE ONLY.
+
+The checker for ``tomosipo_gb300.fdk`` (tomosipo's ``fdk``,
+``tomosipo/astra.py:374-406``), written independently of it: world-space
+ray/plane intersections instead of the kernels' projection matrices, and the
+ramp filter as a direct spatial convolution instead of an FFT. The method is
+Feldkamp, Davis & Kress (J. Opt. Soc. Am. A 1(6), 1984) for flat detectors:
+cosine weights SDD / |X - S|; the Ram-Lak filter h[0] = 1/(4 d^2),
+h[odd n] = -1/(pi^2 n^2 d^2) on the virtual detector through the reference
+point (pitch d = |det_u| SOD / SDD), applied as d * sum_n h[k - n] p[n]; and
+the backprojection sum_t (dbeta_t / 2) (SOD_t / U_t(x))^2 q_t(u, v) with
+bilinear detector reads (zero outside the detector). The reference point is
+the centre of voxel (nz/2, ny/2, nx/2), integer division; dbeta_t are
+central differences of the source's unwrapped angle around the z axis.
+Small cases only (pure NumPy).
+"""
+import math
+
+import numpy as np
+
+
+def _frame(vg, pg):
+    v = pg.to_vec()
+    S, D, U, V = (np.asarray(a, dtype=np.float64) for a in (v.src_pos, v.det_pos, v.det_u, v.det_v))
+    shape = np.array(vg.shape)
+    vs = np.asarray(vg.voxel_sizes, dtype=np.float64).reshape(3)
+    llc = np.asarray(vg.lower_left_corner, dtype=np.float64).reshape(3)
+    ref = llc + (shape // 2 + 0.5) * vs
+    return S, D, U, V, shape, vs, llc, ref
+
+
+def fdk(vg, pg, y):
+    """FDK reconstruction (fp64 volume) of sinogram ``y`` ((rows, angles, cols))."""
+    S, D, U, V, shape, vs, llc, ref = _frame(vg, pg)
+    y = np.asarray(y, dtype=np.float64)
+    R, N, C = y.shape
+    # voxel centres (world)
+    grids = [llc[i] + (np.arange(shape[i]) + 0.5) * vs[i] for i in range(3)]
+    P = np.stack(np.meshgrid(*grids, indexing="ij"), axis=-1).reshape(-1, 3)
+    out = np.zeros(P.shape[0])
+    beta = np.unwrap([math.atan2(s[1] - ref[1], s[2] - ref[2]) for s in S])
+    dbeta = np.abs(np.gradient(beta)) if N > 1 else np.array([2 * math.pi])
+    k = np.arange(-(C - 1), C)
+    h1 = np.zeros(k.shape)  # unit-pitch Ram-Lak kernel, k = -(C-1) .. C-1
+    h1[k == 0] = 0.25
+    odd = k % 2 != 0
+    h1[odd] = -1.0 / (math.pi ** 2 * k[odd].astype(np.float64) ** 2)
+    a = np.arange(R) + 0.5 - R / 2
+    b = np.arange(C) + 0.5 - C / 2
+    for t in range(N):
+        n = np.cross(U[t], V[t])
+        n /= np.linalg.norm(n)
+        if np.dot(D[t] - S[t], n) < 0:
+            n = -n
+        sdd = np.dot(D[t] - S[t], n)
+        sod = np.dot(ref - S[t], n)
+        d = np.linalg.norm(U[t]) * sod / sdd
+        X = D[t] + a[:, None, None] * V[t] + b[None, :, None] * U[t]
+        p = y[:, t, :] * sdd / np.linalg.norm(X - S[t], axis=-1)
+        q = np.stack([np.convolve(p[r], h1)[C - 1:2 * C - 1] for r in range(R)]) / d
+        # project voxel centres: ray S -> P meets the detector plane at X
+        rel = P - S[t]
+        depth = rel @ n
+        Xp = S[t] + rel * (sdd / depth)[:, None]
+        G = np.array([[U[t] @ U[t], U[t] @ V[t]], [U[t] @ V[t], V[t] @ V[t]]])
+        rhs = np.stack([(Xp - D[t]) @ U[t], (Xp - D[t]) @ V[t]], axis=1)
+        uv = np.linalg.solve(G, rhs.T).T  # pixel offsets from the detector centre
+        u = uv[:, 0] + C / 2 - 0.5
+        v = uv[:, 1] + R / 2 - 0.5
+        i0, j0 = np.floor(v).astype(int), np.floor(u).astype(int)
+        fi, fj = v - i0, u - j0
+        val = np.zeros(P.shape[0])
+        for di, wi in ((0, 1 - fi), (1, fi)):
+            for dj, wj in ((0, 1 - fj), (1, fj)):
+                ii, jj = i0 + di, j0 + dj
+                ok = (ii >= 0) & (ii < R) & (jj >= 0) & (jj < C)
+                val[ok] += (wi * wj)[ok] * q[ii[ok], jj[ok]]
+        out += dbeta[t] / 2 * (sod / depth) ** 2 * val
+    return out.reshape(tuple(shape))

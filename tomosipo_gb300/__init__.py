@@ -1,13 +1,16 @@
 """tomosipo_gb300: tomosipo's operator API on hand-written sm_103a CUDA kernels.
 
 ``import tomosipo_gb300 as ts`` gives the names tomosipo exports for the
-projection path (``tomosipo/__init__.py:10-41``): ``operator``, ``volume``,
-``volume_vec``, ``parallel``, ``parallel_vec``, ``cone``, ``cone_vec``, the
-transforms, ``link``, ``to_astra`` / ``from_astra`` and ``epsilon``.
+projection path (``tomosipo/__init__.py:10-41``): ``operator``, ``data``,
+``volume``, ``volume_vec``, ``parallel``, ``parallel_vec``, ``cone``,
+``cone_vec``, the transforms, ``link``, ``to_astra`` / ``from_astra`` and
+``epsilon``; ``tomosipo_gb300.astra`` has the legacy ``forward``/``backward``
+and ``fdk``.
 """
 __version__ = "0.6.0+gb300"
 
 from .Operator import operator, Operator, BackprojectionOperator
+from .Data import data
 from .geometry.volume import volume
 from .geometry.volume_vec import volume_vec
 from . import geometry

@@ -97,6 +97,11 @@ SIGNATURES = {
     "tsgb_sirt_batch_destroy": (ctypes.c_int, [ctypes.c_void_p]),
     "tsgb_projector_get_tuning": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(Tuning)]),
     "tsgb_projector_set_tuning": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(Tuning)]),
+    "tsgb_fdk_backproject": (
+        ctypes.c_int,
+        [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int32,
+         ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p],
+    ),
     "tsgb_last_error": (ctypes.c_char_p, []),
 }
 

@@ -434,11 +434,18 @@ __global__ void bp_bilinear_prep_kernel(const float* __restrict__ sino, float4* 
 // bounds test once its indices are clamped into the padding (positions
 // outside the detector read zeros, as bilinear interpolation with a zero
 // border does); a z-run whose rows all lie inside skips the row clamps.
-template <int kRun, bool kCone>
+// kWeight: kBilParallel, kBilCone (the bilinear backprojector's weights) or
+// kBilFdk: FDK's backprojection weight angle_w[theta] / w^2, where w is the
+// voxel's depth along the detector normal relative to the volume anchor's
+// (the projective denominator pw . [P, 1]).
+enum BilWeight { kBilParallel = 0, kBilCone = 1, kBilFdk = 2 };
+
+template <int kRun, int kWeight>
 __global__ void __launch_bounds__(kBpX* kBpY)
     bp_bilinear_z_kernel(const AngleParams* __restrict__ params, const int* __restrict__ angles,
                          int n_angles, const float4* __restrict__ sinoq, float* __restrict__ vol,
-                         DeviceGeometry g, int additive) {
+                         DeviceGeometry g, int additive, const float* __restrict__ angle_w) {
+  constexpr bool kCone = kWeight == kBilCone;
   const int x = blockIdx.x * kBpX + threadIdx.x;
   const int y = blockIdx.y * kBpY + threadIdx.y;
   const int z0 = blockIdx.z * kRun;
@@ -468,6 +475,7 @@ __global__ void __launch_bounds__(kBpX* kBpY)
     const float vt0 = fmaf(ap.pv[0], zt0, fmaf(ap.pv[1], yt, fmaf(ap.pv[2], xt, ap.pv[3]))) * inw;
     const float dv = ap.pv[0] * inw;
     float K = ap.bil_scale, dxy2 = 0.0f, dz0 = 0.0f;
+    if (kWeight == kBilFdk) K = __ldg(angle_w + theta) * inw * inw;
     if (kCone) {
       K *= inw * inw * inw;
       const float dx = (xt - ap.src[2]) * g.vs[2], dy = (yt - ap.src[1]) * g.vs[1];
@@ -620,11 +628,11 @@ int launch_bp_bilinear(const tsgb_projector* p, float* vol, const float* sino, b
         sino, quads, g);
     const dim3 grid((g.nx + kBpX - 1) / kBpX, (g.ny + kBpY - 1) / kBpY, (g.nz + kRunZ - 1) / kRunZ);
     if (g.kind == TSGB_CONE)
-      bp_bilinear_z_kernel<kRunZ, true><<<grid, block, 0, stream>>>(
-          p->d_params, p->d_bil_fast, p->n_bil_fast, quads, vol, g, additive ? 1 : 0);
+      bp_bilinear_z_kernel<kRunZ, kBilCone><<<grid, block, 0, stream>>>(
+          p->d_params, p->d_bil_fast, p->n_bil_fast, quads, vol, g, additive ? 1 : 0, nullptr);
     else
-      bp_bilinear_z_kernel<kRunZ, false><<<grid, block, 0, stream>>>(
-          p->d_params, p->d_bil_fast, p->n_bil_fast, quads, vol, g, additive ? 1 : 0);
+      bp_bilinear_z_kernel<kRunZ, kBilParallel><<<grid, block, 0, stream>>>(
+          p->d_params, p->d_bil_fast, p->n_bil_fast, quads, vol, g, additive ? 1 : 0, nullptr);
     written = true;
   }
   if (p->n_bil_slow > 0 || !written) {
@@ -633,6 +641,21 @@ int launch_bp_bilinear(const tsgb_projector* p, float* vol, const float* sino, b
     bp_bilinear_kernel<<<grid, block, 0, stream>>>(p->d_params, p->d_bil_slow, p->n_bil_slow, sino,
                                                    vol, g, (additive || written) ? 1 : 0);
   }
+  return int(cudaGetLastError());
+}
+
+int launch_bp_fdk(const tsgb_projector* p, float* vol, const float* sino, const float* angle_w,
+                  bool additive, float* workspace, void* stream_) {
+  cudaStream_t stream = static_cast<cudaStream_t>(stream_);
+  const DeviceGeometry& g = p->g;
+  const long long total = (long long)(g.rows + 2 * kRowPad) * g.nangles * (g.cols + 2 * kColPad);
+  const long long blocks = (total + 255) / 256;
+  float4* quads = reinterpret_cast<float4*>(workspace);
+  bp_bilinear_prep_kernel<<<int(blocks < 152LL * 64 ? blocks : 152LL * 64), 256, 0, stream>>>(
+      sino, quads, g);
+  const dim3 grid((g.nx + kBpX - 1) / kBpX, (g.ny + kBpY - 1) / kBpY, (g.nz + kRunZ - 1) / kRunZ);
+  bp_bilinear_z_kernel<kRunZ, kBilFdk><<<grid, dim3(kBpX, kBpY), 0, stream>>>(
+      p->d_params, p->d_bil_fast, p->n_bil_fast, quads, vol, g, additive ? 1 : 0, angle_w);
   return int(cudaGetLastError());
 }
 

@@ -245,6 +245,26 @@ int tsgb_direct_bp(tsgb_projector* p, float* vol, const float* sino, int32_t add
   return TSGB_OK;
 }
 
+int tsgb_fdk_backproject(tsgb_projector* p, float* vol, const float* filtered, const float* angle_weights,
+                         int32_t additive, void* workspace, int64_t workspace_bytes, void* stream) {
+  g_last_error.clear();
+  if (!p || !vol || !filtered || !angle_weights)
+    return fail(TSGB_ERR_INVALID, "NULL projector or data pointer");
+  if (p->g.kind != TSGB_CONE || p->n_bil_slow > 0 || p->n_bil_fast == 0)
+    return fail(TSGB_ERR_INVALID,
+                "FDK needs a cone beam whose detector v axis runs along z (circular or helical "
+                "scans)");
+  const int64_t need = tsgb_bp_workspace_bytes(p, TSGB_BP_BILINEAR);
+  if (!workspace || workspace_bytes < need)
+    return fail(TSGB_ERR_WORKSPACE, "FDK needs " + std::to_string(need) + " bytes of workspace");
+  int rc = check_device(p);
+  if (rc != TSGB_OK) return rc;
+  cudaError_t e = cudaError_t(tsgb::launch_bp_fdk(p, vol, filtered, angle_weights, additive != 0,
+                                                  static_cast<float*>(workspace), stream));
+  if (e != cudaSuccess) return cuda_fail(e, "FDK backprojection launch");
+  return TSGB_OK;
+}
+
 int tsgb_projector_stats(const tsgb_projector* p, int64_t* out, int32_t n) {
   if (!p || !out || n < 0 || n > 8) return fail(TSGB_ERR_INVALID, "bad stats arguments");
   // FP and matched BP run on the finer detector when it is supersampled, plus

@@ -147,6 +147,11 @@ long long fp_angle_chunk(const DeviceGeometry& g);
 // Default tuning of a new projector whose plan is built (fp.cu).
 tsgb_tuning default_tuning(const tsgb_projector* p);
 
+// FDK backprojection of a weighted, ramp-filtered sinogram (cone beams whose
+// angles all take the z-flat bilinear path; workspace as the bilinear BP's).
+int launch_bp_fdk(const tsgb_projector* p, float* vol, const float* sino, const float* angle_w,
+                  bool additive, float* workspace, void* stream);
+
 // Detector supersampling passes between p's detector and p->fine's (supersample.cu).
 int launch_ss_bin(const tsgb_projector* p, const float* fine, float* coarse, bool additive,
                   void* stream);
