@@ -3,5 +3,6 @@ from .numpy import NumpyLink
 
 try:
     from .torch import TorchLink
+    from .cuda_array import CudaArrayLink
 except ImportError:  # torch missing: NumPy links only
-    TorchLink = None
+    TorchLink = CudaArrayLink = None

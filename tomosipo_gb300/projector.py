@@ -188,7 +188,11 @@ def direct_project(projector, vol_link, proj_link, forward=None, additive=False,
             f"Expected volume {projector.vol_shape} and sinogram {projector.sino_shape}. "
             f"Got {tuple(vol_link.shape)} and {tuple(proj_link.shape)}."
         )
-    vol, sino = vol_link.data, proj_link.data
+    # device-array links (CuPy and the like) project through a torch view
+    vol = getattr(vol_link, "torch_view", None)
+    vol = vol_link.data if vol is None else vol
+    sino = getattr(proj_link, "torch_view", None)
+    sino = proj_link.data if sino is None else sino
     on_gpu = isinstance(vol, torch.Tensor) and vol.is_cuda
     device = vol.device if on_gpu else _cuda_device_for_host_data()
     src, dst = (vol, sino) if forward else (sino, vol)
