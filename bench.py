@@ -322,7 +322,10 @@ def bench_serving(torch, ts, device, n_requests=8, rate=20.0, iterations=20, see
         reqs.append(Request(i, A, y, iterations, float(arrivals[i])))
         updates += 2 * n ** 3 * angles * iterations
     torch.cuda.synchronize()
-    server = SirtServer()
+    # the same requests under the all-jobs-every-step policy, for comparison
+    other = SirtServer(policy="all")
+    st_all = latency_stats(other.run(reqs))
+    server = SirtServer()  # shortest remaining work first (the default)
     t0 = time.perf_counter()
     res = server.run(reqs)
     wall = time.perf_counter() - t0
@@ -339,6 +342,11 @@ def bench_serving(torch, ts, device, n_requests=8, rate=20.0, iterations=20, see
         "max_concurrent_jobs": server.max_concurrent,
         "steps": server.steps,
         "gups": updates / wall / 1e9,
+        "policy": "srpt: per step a work budget of one iteration of the largest job, least "
+                  "remaining work first, several iterations for small jobs",
+        "all_jobs_each_step": {"p50_latency_s": st_all.get("p50_s"),
+                               "p99_latency_s": st_all.get("p99_s"),
+                               "solves_per_s": st_all.get("solves_per_s")},
     }
 
 

@@ -143,6 +143,11 @@ int tsgb_sirt_batch_create(const tsgb_sirt_job* jobs, int32_t n_jobs, tsgb_sirt_
  * branches). */
 int tsgb_sirt_batch_iterate(tsgb_sirt_batch* b, int32_t iterations, void* stream);
 
+/* As tsgb_sirt_batch_iterate, with iterations[i] iterations of job i (the
+ * order of tsgb_sirt_batch_create's ``jobs``; 0 leaves a job as it is), so a
+ * scheduler can advance jobs unevenly from one batch. */
+int tsgb_sirt_batch_iterate_jobs(tsgb_sirt_batch* b, const int32_t* iterations, void* stream);
+
 /* Free a batch's tables (not the jobs' buffers). */
 int tsgb_sirt_batch_destroy(tsgb_sirt_batch* b);
 

@@ -20,13 +20,18 @@ class FakeClock:
 class FakeEngine:
     """Each step takes `step_time`; a job's state counts its iterations."""
 
-    def __init__(self, clock, sizes, step_time=1.0, fail_ids=()):
+    def __init__(self, clock, sizes, step_time=1.0, fail_ids=(), costs=None):
         self.clock, self.sizes, self.step_time = clock, sizes, step_time
         self.fail_ids = set(fail_ids)
+        self.costs = costs or {}
         self.batches = []
+        self.steps = []
 
     def job_bytes(self, req):
         return self.sizes[req.id]
+
+    def job_cost(self, req):
+        return self.costs.get(req.id, 1.0)
 
     def admit(self, req):
         if req.id in self.fail_ids:
@@ -37,10 +42,13 @@ class FakeEngine:
         self.batches.append(sorted(s["id"] for s in states))
         return list(states)
 
-    def step(self, batch):
-        for s in batch:
-            s["iters"] += 1
-        self.clock.t += self.step_time
+    def step(self, batch, iterations):
+        self.steps.append({s["id"]: k for s, k in zip(batch, iterations)})
+        for s, k in zip(batch, iterations):
+            s["iters"] += k
+        # with per-job costs a step takes as long as the work it runs
+        work = sum(k * self.costs.get(s["id"], 1.0) for s, k in zip(batch, iterations))
+        self.clock.t += self.step_time * (max(1.0, work) if self.costs else 1.0)
 
     def result(self, state):
         return state["iters"]
@@ -51,9 +59,10 @@ class FakeEngine:
 
 def _server(sizes, budget, **kw):
     clock = FakeClock()
-    eng = FakeEngine(clock, sizes, **{k: v for k, v in kw.items() if k in ("step_time", "fail_ids")})
-    srv = SirtServer(engine=eng, memory_budget=budget,
-                     max_active=kw.get("max_active", 64))
+    eng = FakeEngine(clock, sizes,
+                     **{k: v for k, v in kw.items() if k in ("step_time", "fail_ids", "costs")})
+    srv = SirtServer(engine=eng, memory_budget=budget, max_active=kw.get("max_active", 64),
+                     policy=kw.get("policy", "all"))
     return clock, eng, srv
 
 
@@ -112,8 +121,8 @@ def test_cancellation_of_waiting_and_running():
     clock2, eng2, srv2 = _server({0: 10}, 100)
 
     class CancelMidway(FakeEngine):
-        def step(self, batch):
-            super().step(batch)
+        def step(self, batch, iterations):
+            super().step(batch, iterations)
             if batch[0]["iters"] == 2:
                 srv2.cancel(0)
 
@@ -130,3 +139,43 @@ def test_latency_stats():
     assert st["p50_s"] == pytest.approx(3.0, abs=0.6)
     assert st["p99_s"] == pytest.approx(5.0, abs=0.1)
     assert st["solves_per_s"] == pytest.approx(2.0)
+
+
+def test_srpt_finishes_small_jobs_first_with_the_same_results():
+    # one large job (cost 8 per iteration) and three small ones (cost 1), 10 iterations each
+    costs = {0: 8.0, 1: 1.0, 2: 1.0, 3: 1.0}
+    reqs = [Request(i, None, None, iterations=10, arrival=0.0) for i in range(4)]
+    out = {}
+    for policy in ("all", "srpt"):
+        clock, eng, srv = _server({i: 1 for i in range(4)}, 100, costs=costs, policy=policy)
+        out[policy] = (srv.run(reqs, clock=clock, sleep=clock.sleep), eng)
+    all_res, srpt_res = out["all"][0], out["srpt"][0]
+    assert [r.x for r in srpt_res] == [r.x for r in all_res] == [10] * 4
+    small_all = sorted(r.latency for r in all_res[1:])
+    small_srpt = sorted(r.latency for r in srpt_res[1:])
+    assert max(small_srpt) < min(small_all)  # every small job finishes earlier
+    assert latency_stats(srpt_res)["p50_s"] < latency_stats(all_res)["p50_s"]
+    # the large job is not starved: makespan within the total work plus the step granularity
+    assert srpt_res[0].latency <= sum(10 * c for c in costs.values()) + 8
+
+
+def test_srpt_plan_respects_budget_and_wait_limit():
+    from tomosipo_gb300.serving import _Active
+
+    srv = SirtServer(engine=FakeEngine(FakeClock(), {}), memory_budget=1, policy="srpt",
+                     max_wait_steps=2)
+
+    def job(i, remaining, cost, waited=0):
+        j = _Active(Request(i, None, None, remaining, 0.0), None, 0, 0.0, cost)
+        j.waited = waited
+        return j
+
+    big, small = job(0, 5, 4.0), job(1, 10, 1.0)
+    assert srv.plan_step([big, small]) == [0, 4]          # budget 4: four small iterations
+    assert srv.plan_step([job(0, 5, 4.0, waited=2), small]) == [1, 4]  # waited too long
+    assert srv.plan_step([big]) == [1]
+    assert srv.plan_step([job(0, 1, 4.0), job(1, 1, 1.0)]) == [0, 1]  # less remaining work first
+    # a forced iteration overdraws the budget: later jobs get 0, never a negative count
+    plan = srv.plan_step([job(0, 9, 4.0, waited=2), job(1, 3, 3.0, waited=0), job(2, 8, 4.0)])
+    assert plan == [0, 1, 0] or min(plan) >= 0
+    assert min(srv.plan_step([job(0, 2, 4.0), job(1, 9, 3.0, waited=3), job(2, 9, 4.0, waited=3)])) >= 0

@@ -94,6 +94,9 @@ SIGNATURES = {
         ctypes.c_int, [ctypes.POINTER(SirtJob), ctypes.c_int32, ctypes.POINTER(ctypes.c_void_p)]
     ),
     "tsgb_sirt_batch_iterate": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, ctypes.c_void_p]),
+    "tsgb_sirt_batch_iterate_jobs": (
+        ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_int32), ctypes.c_void_p]
+    ),
     "tsgb_sirt_batch_destroy": (ctypes.c_int, [ctypes.c_void_p]),
     "tsgb_projector_get_tuning": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(Tuning)]),
     "tsgb_projector_set_tuning": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(Tuning)]),

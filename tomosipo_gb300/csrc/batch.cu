@@ -44,6 +44,7 @@ int bfail(int code, const std::string& msg) {
 struct tsgb_sirt_batch {
   int device = -1;
   std::vector<tsgb_sirt_job> jobs;  // largest first
+  std::vector<int> index;           // jobs[k] is the caller's job index[k]
   std::vector<cudaStream_t> streams;
   std::vector<cudaEvent_t> joins;
   cudaEvent_t fork = nullptr;
@@ -98,7 +99,10 @@ int tsgb_sirt_batch_create(const tsgb_sirt_job* jobs, int32_t n_jobs, tsgb_sirt_
   std::vector<int> order(n_jobs);
   std::iota(order.begin(), order.end(), 0);
   std::stable_sort(order.begin(), order.end(), [&](int a, int c) { return work[a] > work[c]; });
-  for (int i : order) b->jobs.push_back(jobs[i]);
+  for (int i : order) {
+    b->jobs.push_back(jobs[i]);
+    b->index.push_back(i);
+  }
 
   const int n_streams = std::min(n_jobs, kMaxStreams);
   e = cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming);
@@ -119,14 +123,16 @@ int tsgb_sirt_batch_create(const tsgb_sirt_job* jobs, int32_t n_jobs, tsgb_sirt_
   return TSGB_OK;
 }
 
-int tsgb_sirt_batch_iterate(tsgb_sirt_batch* b, int32_t iterations, void* stream_) {
-  tsgb::set_last_error(std::string());
-  if (!b || iterations < 0) return bfail(TSGB_ERR_INVALID, "bad batch or iteration count");
-  int dev = -1;
-  cudaGetDevice(&dev);
-  if (dev != b->device) return bfail(TSGB_ERR_DEVICE, "current device differs from the batch's");
+}  // extern "C"
+
+namespace {
+
+// Iterations count[k] of the batch's job k (its sorted order), forked from and
+// joined back into `stream`.
+int iterate_counts(tsgb_sirt_batch* b, const std::vector<int>& count, cudaStream_t stream) {
+  int iterations = 0;
+  for (int c : count) iterations = std::max(iterations, c);
   if (iterations == 0) return TSGB_OK;
-  cudaStream_t stream = static_cast<cudaStream_t>(stream_);
   const int K = int(b->streams.size());
   cudaError_t e = cudaEventRecord(b->fork, stream);
   for (int k = 0; k < K && e == cudaSuccess; ++k) e = cudaStreamWaitEvent(b->streams[k], b->fork, 0);
@@ -135,6 +141,7 @@ int tsgb_sirt_batch_iterate(tsgb_sirt_batch* b, int32_t iterations, void* stream
   // other.
   for (int it = 0; it < iterations && e == cudaSuccess; ++it) {
     for (size_t i = 0; i < b->jobs.size() && e == cudaSuccess; ++i) {
+      if (it >= count[i]) continue;
       const tsgb_sirt_job& J = b->jobs[i];
       cudaStream_t s = b->streams[i % K];
       const tsgb::FpSirt sirt{J.sino, J.R, J.residual};
@@ -151,6 +158,39 @@ int tsgb_sirt_batch_iterate(tsgb_sirt_batch* b, int32_t iterations, void* stream
   }
   if (e != cudaSuccess) return bfail(TSGB_ERR_CUDA, std::string("batched SIRT launch: ") + cudaGetErrorString(e));
   return TSGB_OK;
+}
+
+int check_batch_device(const tsgb_sirt_batch* b) {
+  int dev = -1;
+  cudaGetDevice(&dev);
+  return dev == b->device ? TSGB_OK
+                          : bfail(TSGB_ERR_DEVICE, "current device differs from the batch's");
+}
+
+}  // namespace
+
+extern "C" {
+
+int tsgb_sirt_batch_iterate(tsgb_sirt_batch* b, int32_t iterations, void* stream) {
+  tsgb::set_last_error(std::string());
+  if (!b || iterations < 0) return bfail(TSGB_ERR_INVALID, "bad batch or iteration count");
+  const int rc = check_batch_device(b);
+  if (rc != TSGB_OK) return rc;
+  return iterate_counts(b, std::vector<int>(b->jobs.size(), iterations),
+                        static_cast<cudaStream_t>(stream));
+}
+
+int tsgb_sirt_batch_iterate_jobs(tsgb_sirt_batch* b, const int32_t* iterations, void* stream) {
+  tsgb::set_last_error(std::string());
+  if (!b || !iterations) return bfail(TSGB_ERR_INVALID, "bad batch or iteration counts");
+  const int rc = check_batch_device(b);
+  if (rc != TSGB_OK) return rc;
+  std::vector<int> count(b->jobs.size());
+  for (size_t k = 0; k < count.size(); ++k) {
+    count[k] = iterations[b->index[k]];
+    if (count[k] < 0) return bfail(TSGB_ERR_INVALID, "negative iteration count");
+  }
+  return iterate_counts(b, count, static_cast<cudaStream_t>(stream));
 }
 
 int tsgb_sirt_batch_destroy(tsgb_sirt_batch* b) {

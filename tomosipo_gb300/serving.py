@@ -2,12 +2,21 @@
 
 Requests (an operator, a measured sinogram and an iteration count) arrive over
 time. The server admits waiting requests first-come-first-served while their
-device memory fits the budget, advances every admitted job by one SIRT
-iteration per step with one batched launch sequence (``NativeBatch``), and
-retires jobs as they finish, so requests that arrive while others run join at
-the next step and their work shares the device with the running jobs. Each
-job's arithmetic is independent of the others in the batch, so a result is
-the same alone and in any mix.
+device memory fits the budget, advances admitted jobs with one batched launch
+sequence per step (``NativeBatch``), and retires jobs as they finish, so
+requests that arrive while others run join at the next step and their work
+shares the device with the running jobs.
+
+Which jobs a step advances is the scheduling policy. ``"srpt"`` (default):
+each step has a work budget of one iteration of the largest active job; jobs
+are taken in order of least remaining work (remaining iterations times the
+per-iteration cost, voxels x angles) and each gets as many iterations as fit,
+so small jobs finish in a few steps instead of waiting for the largest one
+(shortest remaining processing time first, the order that minimises mean
+latency); a job passed over for ``max_wait_steps`` steps gets one iteration
+anyway. ``"all"``: every active job one iteration per step. Each job's
+arithmetic is independent of the others and of the schedule, so a result is
+the same alone, in any mix and under either policy.
 
 There is no counterpart in the reference (its SIRT is a per-job Python loop,
 ``README.md:150-163``). Failure handling is host-side: requests larger than
@@ -53,6 +62,13 @@ class GpuEngine:
 
         return SirtJobState.device_bytes(req.A)
 
+    def job_cost(self, req):
+        """Work of one iteration (voxels x angles; FP + BP scale with it)."""
+        n_vox = 1
+        for d in req.A.domain_shape:
+            n_vox *= int(d)
+        return float(n_vox * req.A.range_shape[1])
+
     def admit(self, req):
         from .sirt import SirtJobState
 
@@ -63,10 +79,10 @@ class GpuEngine:
 
         return NativeBatch(states)
 
-    def step(self, batch):
+    def step(self, batch, iterations):
         import torch
 
-        batch.step(1)
+        batch.step_jobs(iterations)
         torch.cuda.synchronize(batch.device)
 
     def result(self, state):
@@ -78,20 +94,27 @@ class GpuEngine:
 
 
 class _Active:
-    __slots__ = ("req", "state", "remaining", "bytes", "admitted")
+    __slots__ = ("req", "state", "remaining", "bytes", "admitted", "cost", "waited")
 
-    def __init__(self, req, state, nbytes, admitted):
+    def __init__(self, req, state, nbytes, admitted, cost):
         self.req = req
         self.state = state
         self.remaining = req.iterations
         self.bytes = nbytes
         self.admitted = admitted
+        self.cost = cost        # work of one iteration
+        self.waited = 0         # consecutive steps without an iteration
 
 
 class SirtServer:
-    """First-come-first-served admission by memory; one iteration per step."""
+    """First-come-first-served admission by memory; SRPT (or all-jobs) steps."""
 
-    def __init__(self, engine=None, memory_budget=None, max_active=64, memory_fraction=0.8):
+    def __init__(self, engine=None, memory_budget=None, max_active=64, memory_fraction=0.8,
+                 policy="srpt", max_wait_steps=4):
+        if policy not in ("srpt", "all"):
+            raise ValueError(f"policy must be 'srpt' or 'all'. Got {policy!r}")
+        self.policy = policy
+        self.max_wait_steps = int(max_wait_steps)
         self.engine = engine if engine is not None else GpuEngine()
         if memory_budget is None:
             import torch
@@ -104,6 +127,24 @@ class SirtServer:
         self.steps = 0
         self.max_concurrent = 0
         self._cancelled = set()
+
+    def plan_step(self, active):
+        """Iterations each active job runs in the next step (``active`` order)."""
+        if self.policy == "all":
+            return [1] * len(active)
+        left = max(j.cost for j in active)
+        order = sorted(range(len(active)),
+                       key=lambda i: (active[i].remaining * active[i].cost, active[i].req.arrival,
+                                      active[i].req.id))
+        iters = [0] * len(active)
+        for rank, i in enumerate(order):
+            j = active[i]
+            k = max(0, min(j.remaining, int(left // j.cost))) if j.cost > 0 else j.remaining
+            if k == 0 and (rank == 0 or j.waited >= self.max_wait_steps):
+                k = 1
+            iters[i] = k
+            left -= k * j.cost
+        return iters
 
     def cancel(self, req_id):
         """Cancel a waiting or running request (takes effect at the next step)."""
@@ -173,7 +214,7 @@ class SirtServer:
                     results[req.id].finished = now()
                     continue
                 self.used += need
-                job = _Active(req, state, need, now())
+                job = _Active(req, state, need, now(), float(self.engine.job_cost(req)))
                 results[req.id].admitted = job.admitted
                 active.append(job)
                 changed = True
@@ -192,10 +233,12 @@ class SirtServer:
                 batch = self.engine.build([j.state for j in active])
                 changed = False
             self.max_concurrent = max(self.max_concurrent, len(active))
-            self.engine.step(batch)
+            iters = self.plan_step(active)
+            self.engine.step(batch, iters)
             self.steps += 1
-            for job in list(active):
-                job.remaining -= 1
+            for job, k in zip(list(active), iters):
+                job.remaining -= k
+                job.waited = 0 if k else job.waited + 1
                 if job.remaining <= 0:
                     retire(job, "done", self.engine.result(job.state))
         self.engine.release(batch)

@@ -114,6 +114,15 @@ class NativeBatch:
             _native.check(lib.tsgb_sirt_batch_iterate(self._batch, int(iterations), stream),
                           "tsgb_sirt_batch_iterate")
 
+    def step_jobs(self, iterations):
+        """``iterations[i]`` iterations of job i (creation order) on the current stream."""
+        lib = _native.load()
+        counts = (ctypes.c_int32 * len(self.states))(*[int(k) for k in iterations])
+        with torch.cuda.device(self.device):
+            stream = torch.cuda.current_stream(self.device).cuda_stream
+            _native.check(lib.tsgb_sirt_batch_iterate_jobs(self._batch, counts, stream),
+                          "tsgb_sirt_batch_iterate_jobs")
+
     def close(self):
         if getattr(self, "_batch", None):
             _native.load().tsgb_sirt_batch_destroy(self._batch)
