@@ -192,3 +192,32 @@ def test_numpy_and_torch_inputs_agree(device):
     assert isinstance(y_np, np.ndarray)
     assert np.abs(y_np - y_t).sum() == pytest.approx(0.0)
     assert np.abs(A.T(y_np) - A.T(torch.from_numpy(y_t).to(device)).cpu().numpy()).sum() == pytest.approx(0.0, abs=1e-3)
+
+
+def test_wide_sinogram_paths_by_linearity(device):
+    """Maximum sizes: a sinogram of more than 2^31 detector pixels (with padding)
+    takes the 64-bit-offset paths of the forward projector's output, the row-pair
+    backprojector and the general bilinear backprojector. Splitting the angles in
+    two halves gives operators below that size (32-bit paths): the forward
+    projections must agree bit for bit per angle, and the backprojection must be
+    the sum of the halves' within TOL_ORACLE. The two sums add the same ~12,000
+    fp32 terms per voxel in different orders, which alone differs by ~2e-6; an
+    offset error would be of order one."""
+    vg = ts.volume(shape=32, size=1)
+    pg = ts.cone(angles=2048, shape=(1024, 1040), size=1.5, cone_angle=0.3)
+    rows, cols = pg.det_shape
+    assert (rows + 4) * pg.num_angles * cols >= 2 ** 31
+    A = ts.operator(vg, pg)
+    A1, A2 = ts.operator(vg, pg[:1024]), ts.operator(vg, pg[1024:])
+    x = torch.from_numpy(noise_cube_phantom(vg.shape, seed=9)).to(device)
+    y = A(x)
+    assert torch.equal(y[:, :1024], A1(x)) and torch.equal(y[:, 1024:], A2(x))
+    bp = A.T(y)
+    bp_split = A1.T(y[:, :1024].contiguous()) + A2.T(y[:, 1024:].contiguous())
+    assert rel_l2(bp.cpu().numpy(), bp_split.cpu().numpy()) <= TOL_ORACLE
+    B, B1, B2 = (ts.operator(vg, g, backprojector="bilinear") for g in (pg, pg[:1024], pg[1024:]))
+    bb = B.T(y)
+    bb_split = B1.T(y[:, :1024].contiguous()) + B2.T(y[:, 1024:].contiguous())
+    assert rel_l2(bb.cpu().numpy(), bb_split.cpu().numpy()) <= TOL_ORACLE
+    del y, bp, bb
+    torch.cuda.empty_cache()
