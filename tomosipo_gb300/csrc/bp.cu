@@ -151,18 +151,31 @@ __device__ __forceinline__ void bp_sep_accumulate(const AngleParams* __restrict_
         const float2* __restrict__ colv = col + Offset(g.ov) * rs;  // row 0 of this column
         // vs is monotone in j: if both ends select rows inside [vmin, vmax]
         // every voxel does, and no clamping is needed (NaN fails the test).
+        // Otherwise rows outside [-kRowPad, rows] hold zeros either way:
+        // clamping keeps both reads inside the padding (NaN clamps to the low
+        // end). Two loops behind a per-column branch (nearly every column is
+        // inside) beat one loop with predicated clamps by 14 %.
         const bool inside = fminf(vs0, vs1) >= vmin && fmaxf(vs0, vs1) < vmax + 1.0f;
+        if (inside) {
 #pragma unroll
-        for (int j = 0; j < kRun; ++j) {
-          float v0 = floorf(fmaf(float(j), inv, vs0));
-          // Rows outside [-kRowPad, rows] hold zeros either way: clamping
-          // keeps both reads inside the padding (NaN clamps to the low end).
-          if (!inside) v0 = fminf(fmaxf(v0, vmin), vmax);
-          const float at0 = fabsf(fmaf(v0, Sl, C0) - float(j));
-          const float2 yy = __ldg(colv + Offset((int)v0) * rs);
-          const float V = fmaf(fmaxf(0.0f, 1.0f - at0), yy.x, fmaxf(0.0f, c1s + at0) * yy.y);
+          for (int j = 0; j < kRun; ++j) {
+            const float v0 = floorf(fmaf(float(j), inv, vs0));
+            const float at0 = fabsf(fmaf(v0, Sl, C0) - float(j));
+            const float2 yy = __ldg(colv + Offset((int)v0) * rs);
+            const float V = fmaf(fmaxf(0.0f, 1.0f - at0), yy.x, fmaxf(0.0f, c1s + at0) * yy.y);
 #pragma unroll
-          for (int m = 0; m < kA; ++m) acc[m][j] = fmaf(h[m], V, acc[m][j]);
+            for (int m = 0; m < kA; ++m) acc[m][j] = fmaf(h[m], V, acc[m][j]);
+          }
+        } else {
+#pragma unroll
+          for (int j = 0; j < kRun; ++j) {
+            const float v0 = fminf(fmaxf(floorf(fmaf(float(j), inv, vs0)), vmin), vmax);
+            const float at0 = fabsf(fmaf(v0, Sl, C0) - float(j));
+            const float2 yy = __ldg(colv + Offset((int)v0) * rs);
+            const float V = fmaf(fmaxf(0.0f, 1.0f - at0), yy.x, fmaxf(0.0f, c1s + at0) * yy.y);
+#pragma unroll
+            for (int m = 0; m < kA; ++m) acc[m][j] = fmaf(h[m], V, acc[m][j]);
+          }
         }
       } else {
 #pragma unroll
@@ -434,6 +447,28 @@ __global__ void bp_bilinear_prep_kernel(const float* __restrict__ sino, float4* 
 // bounds test once its indices are clamped into the padding (positions
 // outside the detector read zeros, as bilinear interpolation with a zero
 // border does); a z-run whose rows all lie inside skips the row clamps.
+// One voxel's term of the z-flat bilinear backprojection: the quad at row
+// floor(vt) of the column (clamped into the zero padding when `clamp`),
+// interpolated, times the weight (for cone beams K times the source distance).
+template <bool kCone>
+__device__ __forceinline__ float bilinear_z_term(const float4* __restrict__ colq, int rs, float vt,
+                                                 float vmin, float vmax, bool clamp, float fu,
+                                                 float K, float dz, float dxy2, float acc) {
+  float fv0 = floorf(vt);
+  const float fv = vt - fv0;
+  if (clamp) fv0 = fminf(fmaxf(fv0, vmin), vmax);  // rows outside read the zero padding
+  const float4 q = __ldg(colq + (int)fv0 * rs);
+  const float top = fmaf(fu, q.y - q.x, q.x);
+  const float bot = fmaf(fu, q.w - q.z, q.z);
+  const float val = fmaf(fv, bot - top, top);
+  float c = K;
+  if (kCone) {
+    const float l2 = fmaf(dz, dz, dxy2);
+    c *= l2 * rsqrtf(l2);
+  }
+  return fmaf(c, val, acc);
+}
+
 // kWeight: kBilParallel, kBilCone (the bilinear backprojector's weights) or
 // kBilFdk: FDK's backprojection weight angle_w[theta] / w^2, where w is the
 // voxel's depth along the detector normal relative to the volume anchor's
@@ -486,23 +521,17 @@ __global__ void __launch_bounds__(kBpX* kBpY)
     // vt is monotone in j: if both ends read rows inside [vmin, vmax] so does
     // every voxel (NaN fails the test and takes the clamped loop).
     const bool inside = fminf(vt0, vt1) >= vmin && fmaxf(vt0, vt1) < vmax + 1.0f;
+    // one loop per case behind a per-column branch (see bp_sep_accumulate)
+    if (inside) {
 #pragma unroll
-    for (int j = 0; j < kRun; ++j) {
-      const float vt = fmaf(float(j), dv, vt0);
-      float fv0 = floorf(vt);
-      const float fv = vt - fv0;
-      if (!inside) fv0 = fminf(fmaxf(fv0, vmin), vmax);  // rows outside read the zero padding
-      const float4 q = __ldg(colq + (int)fv0 * rs);
-      const float top = fmaf(fu, q.y - q.x, q.x);
-      const float bot = fmaf(fu, q.w - q.z, q.z);
-      const float val = fmaf(fv, bot - top, top);
-      float c = K;
-      if (kCone) {
-        const float dz = fmaf(float(j), g.vs[0], dz0);
-        const float l2 = fmaf(dz, dz, dxy2);
-        c *= l2 * rsqrtf(l2);
-      }
-      acc[j] = fmaf(c, val, acc[j]);
+      for (int j = 0; j < kRun; ++j)
+        acc[j] = bilinear_z_term<kCone>(colq, rs, fmaf(float(j), dv, vt0), vmin, vmax, false, fu,
+                                        K, fmaf(float(j), g.vs[0], dz0), dxy2, acc[j]);
+    } else {
+#pragma unroll
+      for (int j = 0; j < kRun; ++j)
+        acc[j] = bilinear_z_term<kCone>(colq, rs, fmaf(float(j), dv, vt0), vmin, vmax, true, fu,
+                                        K, fmaf(float(j), g.vs[0], dz0), dxy2, acc[j]);
     }
   }
 #pragma unroll
