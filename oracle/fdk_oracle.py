@@ -1,6 +1,6 @@
 """FP64 NumPy FDK -- TEST INFRASTRUCTURE ONLY.
 
-The checker for ``tomosipo_gb300.fdk`` (tomosipo's ``fdk``,
+The oracle for ``tomosipo_gb300.fdk`` (tomosipo's ``fdk``,
 ``tomosipo/astra.py:374-406``), written independently of it: world-space
 ray/plane intersections instead of the kernels' projection matrices, and the
 ramp filter as a direct spatial convolution instead of an FFT. The method is
