@@ -1,8 +1,8 @@
 // FP64 CPU oracle of the tomosipo_gb300 projector -- TEST INFRASTRUCTURE ONLY.
 //
 // Only the tests, the smoke check and the CPU-baseline leg of bench.py use
-// this file, as the reference the results are compared with and as the timed CPU baseline. The product path
-// never calls it.
+// this file, as the reference the results are compared with and as the timed
+// CPU baseline. The product path never calls it.
 //
 // What it restates. tomosipo delegates A(x) / A.T(y) to ASTRA's cuda3d
 // projector (tomosipo/astra.py:80-98, 147-153); ASTRA is a third-party
