@@ -8,11 +8,17 @@
 // angle's (d, a, b) frame receives W * y * tent(q_a - i) * tent(q_b - j) from
 // every ray whose plane-k sample lies within one voxel of it.
 //  1. bp_weight_kernel premultiplies the sinogram by each ray's plane step W
-//     (the same W the forward projector applies).
+//     (the same W the forward projector applies) and stores it as row pairs,
+//     (W y[v], W y[v+1]) per pixel, with zero padding rows.
 //  2. bp_separable_kernel handles angles whose det_v lies along z (b = z):
-//     q_a then depends on the column only, so each thread solves once per
-//     angle for the columns that reach its voxel column and walks a run of
-//     J voxels along z, each needing a short range of detector rows.
+//     q_a then depends on the column only, and on a plane of the dominant
+//     axis a detector column's vertical profile does not depend on the
+//     voxel's in-plane position. A thread owns two voxel columns adjacent
+//     along the in-plane axis a and 16 voxels along z; per angle it solves
+//     once for the columns that reach either and builds each column's
+//     profile once per voxel, from one row-pair load. a is x for some angles
+//     and y for others, so the angles run in two passes with different
+//     thread-to-voxel mappings, the second adding onto the first.
 //  3. bp_general_kernel handles every other angle: it projects the corners of
 //     the voxel's tent footprint onto the detector and tests every pixel in
 //     their bounding box with the forward projector's own ray formula.
@@ -20,7 +26,9 @@
 // Bilinear backprojection: voxel-driven, bilinear interpolation of the
 // detector at the projected voxel centre, weighted so that it approximates
 // the transpose (voxel volume / pixel area / ray obliquity, times the cone
-// magnification squared).
+// magnification squared). For z-flat geometries a quad copy of the sinogram
+// gives each voxel its four taps in one load; the same kernel with FDK's
+// weights is the backprojection of the FDK reconstruction.
 #include <cuda_runtime.h>
 
 #include <type_traits>

@@ -4,17 +4,19 @@
 // ``astra.experimental.direct_FPBP3D(..., "FP")`` (tomosipo/astra.py:147-153).
 //
 // Data flow per call:
-//  1. fp_layout_kernel writes, for every axis permutation (d, a, b) the angles
-//     use, a zero-padded copy of the volume laid out [d][a][b] (b fastest).
-//  2. fp_ray_kernel: one thread per (angle, row, column) walks the planes of
-//     the dominant axis, samples bilinearly and scales by the plane step.
-//     A warp is 32 consecutive detector rows of one column. b is the volume
-//     axis det_v runs along, so the warp's samples on a plane lie on one short
-//     run along b (contiguous in the copy); for circular and helical
-//     geometries (det_v along z) all lanes also share the same two a columns.
-//     Blocks are ordered row-fastest, then column, then angle. (Ordering by
-//     row band across angles keeps a volume slab in L2 and wins at 384^3,
-//     but measured slower at 512^3 / 1024 angles, the headline size.)
+//  1. fp_layout_transpose_kernel / fp_layout_kernel write, for every axis
+//     permutation (d, a, b) the angles use, a zero-padded copy of the volume
+//     laid out [d][a][b] (b fastest), as single voxels or as neighbour pairs
+//     along b (the projector's tuning).
+//  2. fp_ray_kernel: one thread per (row, column) and pair of adjacent angles
+//     walks the planes of the dominant axis for both rays, samples
+//     bilinearly and scales by the plane step. A warp is 32 consecutive
+//     detector rows of one column. b is the volume axis det_v runs along, so
+//     the warp's samples on a plane lie on one short run along b (contiguous
+//     in the copy); for circular and helical geometries (det_v along z) all
+//     lanes also share the same two a columns. Tiles run in the order of the
+//     projector's schedule: groups of angle pairs over detector patches, so
+//     the volume slab a group crosses stays in L2 (fp_schedule_tile).
 #include <cuda_runtime.h>
 
 #include <algorithm>
