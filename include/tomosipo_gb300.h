@@ -93,6 +93,32 @@ int tsgb_direct_bp(tsgb_projector* p, float* vol, const float* sino,
                    int32_t additive, int32_t bp_kind, void* workspace,
                    int64_t workspace_bytes, void* stream);
 
+/* Forward projection of the angles angle_begin .. angle_end - 1 only, into
+ * their slices of the full sinogram (other angles untouched). With
+ * copies_ready != 0 the padded volume copies a previous call on the same
+ * volume left in the workspace are reused. Together with
+ * tsgb_copy_sino_angles this lets a caller stream the sinogram to the host
+ * while later angles are projected. Results equal tsgb_direct_fp's. Not for
+ * projectors with detector supersampling. No counterpart in the reference. */
+int tsgb_direct_fp_angles(tsgb_projector* p, const float* vol, float* sino, int32_t additive,
+                          int64_t angle_begin, int64_t angle_end, int32_t copies_ready,
+                          void* workspace, int64_t workspace_bytes, void* stream);
+
+/* Matched backprojection of the angles angle_begin .. angle_end - 1 of sino
+ * (the full sinogram; other angles are not read), vol = ... or vol += ...
+ * when ``additive``: a caller can backproject angle chunks as they arrive
+ * from the host. The sum over chunks equals tsgb_direct_bp's up to fp32
+ * summation order. Not for projectors with detector supersampling. */
+int tsgb_direct_bp_angles(tsgb_projector* p, float* vol, const float* sino, int32_t additive,
+                          int64_t angle_begin, int64_t angle_end, void* workspace,
+                          int64_t workspace_bytes, void* stream);
+
+/* Copy the angles angle_begin .. angle_end - 1 of a rows x num_angles x cols
+ * float32 sinogram between host and device (direction from the pointers;
+ * asynchronous when the host memory is pinned), one strided 2-D copy. */
+int tsgb_copy_sino_angles(void* dst, const void* src, int64_t rows, int64_t num_angles,
+                          int64_t cols, int64_t angle_begin, int64_t angle_end, void* stream);
+
 /* Forward projection sino = A(vol) (sino += ... when ``additive``) that allocates
  * no device memory, for callers that cannot call cudaMalloc: code running inside
  * another framework's allocator (a custom-call hook) or a real-time loop with a

@@ -31,7 +31,9 @@
 // weights is the backprojection of the FDK reconstruction.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <type_traits>
+#include <vector>
 
 #include "device_common.cuh"
 
@@ -562,11 +564,9 @@ namespace {
 constexpr int kSepA = 2;  // voxel columns per thread along a (matched)
 
 template <bool kWide, bool kAisX, int kMode>
-void launch_sep_pass_t(const tsgb_projector* p, const float2* pairs, float* vol, const float* C,
-                       float* scratch, cudaStream_t stream) {
+void launch_sep_pass_t(const tsgb_projector* p, const int* angles, int n, const float2* pairs,
+                       float* vol, const float* C, float* scratch, cudaStream_t stream) {
   const DeviceGeometry& g = p->g;
-  const int* angles = p->d_sep_angles + (kAisX ? 0 : p->n_sep_ax);
-  const int n = kAisX ? p->n_sep_ax : p->n_separable_bp - p->n_sep_ax;
   const int tx = kBpX * (kAisX ? kSepA : 1), ty = kBpY * (kAisX ? 1 : kSepA);
   const dim3 grid((g.nx + tx - 1) / tx, (g.ny + ty - 1) / ty, (g.nz + kRunZ - 1) / kRunZ);
   bp_separable_kernel<kSepA, kRunZ, kWide, kAisX, kMode><<<grid, dim3(kBpX, kBpY), 0, stream>>>(
@@ -574,41 +574,65 @@ void launch_sep_pass_t(const tsgb_projector* p, const float2* pairs, float* vol,
 }
 
 template <bool kWide, bool kAisX>
-void launch_sep_pass_m(const tsgb_projector* p, int mode, const float2* pairs, float* vol,
-                       const float* C, float* scratch, cudaStream_t stream) {
+void launch_sep_pass_m(const tsgb_projector* p, const int* angles, int n, int mode,
+                       const float2* pairs, float* vol, const float* C, float* scratch,
+                       cudaStream_t stream) {
   switch (mode) {
-    case kBpSet: launch_sep_pass_t<kWide, kAisX, kBpSet>(p, pairs, vol, C, scratch, stream); break;
-    case kBpAdd: launch_sep_pass_t<kWide, kAisX, kBpAdd>(p, pairs, vol, C, scratch, stream); break;
-    case kBpSirtFirst:
-      launch_sep_pass_t<kWide, kAisX, kBpSirtFirst>(p, pairs, vol, C, scratch, stream);
+    case kBpSet:
+      launch_sep_pass_t<kWide, kAisX, kBpSet>(p, angles, n, pairs, vol, C, scratch, stream);
       break;
-    default: launch_sep_pass_t<kWide, kAisX, kBpSirtLast>(p, pairs, vol, C, scratch, stream);
+    case kBpAdd:
+      launch_sep_pass_t<kWide, kAisX, kBpAdd>(p, angles, n, pairs, vol, C, scratch, stream);
+      break;
+    case kBpSirtFirst:
+      launch_sep_pass_t<kWide, kAisX, kBpSirtFirst>(p, angles, n, pairs, vol, C, scratch, stream);
+      break;
+    default:
+      launch_sep_pass_t<kWide, kAisX, kBpSirtLast>(p, angles, n, pairs, vol, C, scratch, stream);
   }
 }
 
-// One pass of the separable matched backprojection (a = x or a = y angles).
-void launch_sep_pass(const tsgb_projector* p, bool a_is_x, int mode, const float2* pairs,
-                     float* vol, const float* C, float* scratch, cudaStream_t stream) {
+// One pass of the separable matched backprojection over the n angle ids at
+// `angles` (device), all with in-plane axis x (a_is_x) or all with y.
+void launch_sep_pass(const tsgb_projector* p, bool a_is_x, const int* angles, int n, int mode,
+                     const float2* pairs, float* vol, const float* C, float* scratch,
+                     cudaStream_t stream) {
   const DeviceGeometry& g = p->g;
   const bool wide = (size_t)(g.rows + 2 * kRowPad) * g.nangles * g.cols >= (size_t(1) << 31);
-  if (wide && a_is_x) launch_sep_pass_m<true, true>(p, mode, pairs, vol, C, scratch, stream);
-  else if (wide) launch_sep_pass_m<true, false>(p, mode, pairs, vol, C, scratch, stream);
-  else if (a_is_x) launch_sep_pass_m<false, true>(p, mode, pairs, vol, C, scratch, stream);
-  else launch_sep_pass_m<false, false>(p, mode, pairs, vol, C, scratch, stream);
+  if (wide && a_is_x)
+    launch_sep_pass_m<true, true>(p, angles, n, mode, pairs, vol, C, scratch, stream);
+  else if (wide)
+    launch_sep_pass_m<true, false>(p, angles, n, mode, pairs, vol, C, scratch, stream);
+  else if (a_is_x)
+    launch_sep_pass_m<false, true>(p, angles, n, mode, pairs, vol, C, scratch, stream);
+  else
+    launch_sep_pass_m<false, false>(p, angles, n, mode, pairs, vol, C, scratch, stream);
+}
+
+// Entries of host_list[lo, hi) (angle ids in increasing order) that lie in
+// [a0, a1): offset into the list and count.
+void angle_sub_range(const std::vector<int>& host_list, int lo, int hi, int a0, int a1, int& off,
+                     int& n) {
+  const auto b = host_list.begin();
+  const auto first = std::lower_bound(b + lo, b + hi, a0);
+  const auto last = std::lower_bound(first, b + hi, a1);
+  off = int(first - b);
+  n = int(last - first);
 }
 
 }  // namespace
 
 int launch_bp_matched(const tsgb_projector* p, float* vol, const float* sino, bool additive,
-                      float* workspace, void* stream_) {
+                      float* workspace, void* stream_, int angle_begin, int angle_end) {
   cudaStream_t stream = static_cast<cudaStream_t>(stream_);
   const DeviceGeometry& g = p->g;
+  if (angle_end < 0) angle_end = g.nangles;
   float2* pairs = reinterpret_cast<float2*>(workspace);
   const size_t rs = (size_t)g.nangles * g.cols;  // elements between rows
   {
     const dim3 block(32, 8);
-    for (int a0 = 0; a0 < g.nangles; a0 += 65535) {
-      const int n = g.nangles - a0 < 65535 ? g.nangles - a0 : 65535;
+    for (int a0 = angle_begin; a0 < angle_end; a0 += 65535) {
+      const int n = angle_end - a0 < 65535 ? angle_end - a0 : 65535;
       const dim3 grid((g.cols + 31) / 32, (g.rows + 1 + 7) / 8, n);
       // offset the angle through the pointers: rows are strided by nangles*cols
       bp_weight_kernel<<<grid, block, 0, stream>>>(p->d_params + a0, p->d_columns + (size_t)a0 * g.cols,
@@ -620,18 +644,24 @@ int launch_bp_matched(const tsgb_projector* p, float* vol, const float* sino, bo
   // rows .. rows + kRowPad - 1
   cudaMemsetAsync(pairs, 0, (kRowPad - 1) * rs * sizeof(float2), stream);
   cudaMemsetAsync(pairs + (kRowPad + g.rows) * rs, 0, kRowPad * rs * sizeof(float2), stream);
-  const int n_ax = p->n_sep_ax, n_ay = p->n_separable_bp - p->n_sep_ax;
+  // the angles of [angle_begin, angle_end) in each of the three angle lists
+  int off_x, n_ax, off_y, n_ay, off_g, n_g;
+  angle_sub_range(p->host_sep_angles, 0, p->n_sep_ax, angle_begin, angle_end, off_x, n_ax);
+  angle_sub_range(p->host_sep_angles, p->n_sep_ax, p->n_separable_bp, angle_begin, angle_end,
+                  off_y, n_ay);
+  angle_sub_range(p->host_gen_angles, 0, p->n_general_bp, angle_begin, angle_end, off_g, n_g);
   if (n_ax > 0)
-    launch_sep_pass(p, true, additive ? kBpAdd : kBpSet, pairs, vol, nullptr, nullptr, stream);
+    launch_sep_pass(p, true, p->d_sep_angles + off_x, n_ax, additive ? kBpAdd : kBpSet, pairs,
+                    vol, nullptr, nullptr, stream);
   if (n_ay > 0)
-    launch_sep_pass(p, false, (additive || n_ax > 0) ? kBpAdd : kBpSet, pairs, vol, nullptr,
-                    nullptr, stream);
-  const bool written = p->n_separable_bp > 0;
-  if (p->n_general_bp > 0 || !written) {
+    launch_sep_pass(p, false, p->d_sep_angles + off_y, n_ay,
+                    (additive || n_ax > 0) ? kBpAdd : kBpSet, pairs, vol, nullptr, nullptr, stream);
+  const bool written = n_ax + n_ay > 0;
+  if (n_g > 0 || (!written && !additive)) {
     const dim3 block(32, 4);
     const dim3 grid((g.nx + 31) / 32, (g.ny + 3) / 4, g.nz);
-    bp_general_kernel<<<grid, block, 0, stream>>>(p->d_params, p->d_columns, p->d_gen_angles,
-                                                  p->n_general_bp, pairs, vol, g,
+    bp_general_kernel<<<grid, block, 0, stream>>>(p->d_params, p->d_columns,
+                                                  p->d_gen_angles + off_g, n_g, pairs, vol, g,
                                                   (additive || written) ? 1 : 0);
   }
   return int(cudaGetLastError());
@@ -642,11 +672,15 @@ int launch_bp_sirt(const tsgb_projector* p, float* vol, const float* C, const fl
   cudaStream_t stream = static_cast<cudaStream_t>(stream_);
   const float2* pairs = reinterpret_cast<const float2*>(res);
   const int n_ax = p->n_sep_ax, n_ay = p->n_separable_bp - p->n_sep_ax;
+  const int* ax = p->d_sep_angles;
+  const int* ay = p->d_sep_angles + n_ax;
   if (n_ax > 0 && n_ay > 0) {
-    launch_sep_pass(p, true, kBpSirtFirst, pairs, vol, C, scratch, stream);
-    launch_sep_pass(p, false, kBpSirtLast, pairs, vol, C, scratch, stream);
-  } else if (n_ax > 0 || n_ay > 0) {
-    launch_sep_pass(p, n_ax > 0, kBpSirtLast, pairs, vol, C, nullptr, stream);
+    launch_sep_pass(p, true, ax, n_ax, kBpSirtFirst, pairs, vol, C, scratch, stream);
+    launch_sep_pass(p, false, ay, n_ay, kBpSirtLast, pairs, vol, C, scratch, stream);
+  } else if (n_ax > 0) {
+    launch_sep_pass(p, true, ax, n_ax, kBpSirtLast, pairs, vol, C, nullptr, stream);
+  } else if (n_ay > 0) {
+    launch_sep_pass(p, false, ay, n_ay, kBpSirtLast, pairs, vol, C, nullptr, stream);
   }
   return int(cudaGetLastError());
 }

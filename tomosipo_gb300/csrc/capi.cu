@@ -117,6 +117,8 @@ int tsgb_projector_create(const tsgb_volume_desc* vol, const tsgb_projection_des
   cudaError_t e = cudaGetDevice(&p->device);
   if (e == cudaSuccess) e = upload(&p->d_params, p->host_params);
   if (e == cudaSuccess) e = upload(&p->d_columns, columns);
+  p->host_sep_angles = sep;
+  p->host_gen_angles = gen;
   if (e == cudaSuccess) e = upload(&p->d_sep_angles, sep);
   if (e == cudaSuccess) e = upload(&p->d_gen_angles, gen);
   if (e == cudaSuccess) e = upload(&p->d_bil_fast, bfast);
@@ -242,6 +244,65 @@ int tsgb_direct_bp(tsgb_projector* p, float* vol, const float* sino, int32_t add
     e = cudaError_t(tsgb::launch_bp_bilinear(p, vol, sino, additive != 0,
                                              static_cast<float*>(workspace), stream));
   if (e != cudaSuccess) return cuda_fail(e, "backprojection launch");
+  return TSGB_OK;
+}
+
+int tsgb_direct_fp_angles(tsgb_projector* p, const float* vol, float* sino, int32_t additive,
+                          int64_t angle_begin, int64_t angle_end, int32_t copies_ready,
+                          void* workspace, int64_t workspace_bytes, void* stream) {
+  g_last_error.clear();
+  if (!p || !vol || !sino) return fail(TSGB_ERR_INVALID, "NULL projector or data pointer");
+  if (p->fine) return fail(TSGB_ERR_INVALID, "angle ranges need detector supersampling 1");
+  if (angle_begin < 0 || angle_end > p->g.nangles || angle_begin >= angle_end)
+    return fail(TSGB_ERR_INVALID, "angle range outside 0 .. num_angles");
+  const int64_t need = tsgb_fp_workspace_bytes(p);
+  if (need > 0 && (!workspace || workspace_bytes < need))
+    return fail(TSGB_ERR_WORKSPACE, "forward projection needs " + std::to_string(need) +
+                                        " bytes of workspace");
+  int rc = check_device(p);
+  if (rc != TSGB_OK) return rc;
+  cudaError_t e = cudaError_t(tsgb::launch_fp(p, vol, sino, additive != 0,
+                                              static_cast<float*>(workspace), stream, nullptr,
+                                              int(angle_begin), int(angle_end), copies_ready != 0));
+  if (e != cudaSuccess) return cuda_fail(e, "forward projection launch");
+  return TSGB_OK;
+}
+
+int tsgb_direct_bp_angles(tsgb_projector* p, float* vol, const float* sino, int32_t additive,
+                          int64_t angle_begin, int64_t angle_end, void* workspace,
+                          int64_t workspace_bytes, void* stream) {
+  g_last_error.clear();
+  if (!p || !vol || !sino) return fail(TSGB_ERR_INVALID, "NULL projector or data pointer");
+  if (p->fine) return fail(TSGB_ERR_INVALID, "angle ranges need detector supersampling 1");
+  if (angle_begin < 0 || angle_end > p->g.nangles || angle_begin >= angle_end)
+    return fail(TSGB_ERR_INVALID, "angle range outside 0 .. num_angles");
+  const int64_t need = tsgb_bp_workspace_bytes(p, TSGB_BP_MATCHED);
+  if (need > 0 && (!workspace || workspace_bytes < need))
+    return fail(TSGB_ERR_WORKSPACE,
+                "backprojection needs " + std::to_string(need) + " bytes of workspace");
+  int rc = check_device(p);
+  if (rc != TSGB_OK) return rc;
+  cudaError_t e = cudaError_t(tsgb::launch_bp_matched(p, vol, sino, additive != 0,
+                                                      static_cast<float*>(workspace), stream,
+                                                      int(angle_begin), int(angle_end)));
+  if (e != cudaSuccess) return cuda_fail(e, "backprojection launch");
+  return TSGB_OK;
+}
+
+int tsgb_copy_sino_angles(void* dst, const void* src, int64_t rows, int64_t num_angles,
+                          int64_t cols, int64_t angle_begin, int64_t angle_end, void* stream) {
+  g_last_error.clear();
+  if (!dst || !src || rows < 1 || cols < 1 || angle_begin < 0 || angle_end > num_angles ||
+      angle_begin >= angle_end)
+    return fail(TSGB_ERR_INVALID, "bad sinogram copy arguments");
+  const size_t pitch = size_t(num_angles) * cols * sizeof(float);
+  const size_t off = size_t(angle_begin) * cols * sizeof(float);
+  cudaError_t e = cudaMemcpy2DAsync(static_cast<char*>(dst) + off, pitch,
+                                    static_cast<const char*>(src) + off, pitch,
+                                    size_t(angle_end - angle_begin) * cols * sizeof(float),
+                                    size_t(rows), cudaMemcpyDefault,
+                                    static_cast<cudaStream_t>(stream));
+  if (e != cudaSuccess) return cuda_fail(e, "sinogram copy");
   return TSGB_OK;
 }
 

@@ -326,7 +326,7 @@ template <bool kSirt, typename E>
 __global__ void __launch_bounds__(kFpRows* kFpCols, 4)
     fp_ray_kernel(const AngleParams* __restrict__ params, const ColumnEntry* __restrict__ columns,
                   const E* __restrict__ ws, float* __restrict__ sino, DeviceGeometry g,
-                  FpSchedule sched, int angle0, int additive, FpSirt sirt) {
+                  FpSchedule sched, int angle0, int angle_end, int additive, FpSirt sirt) {
   __shared__ volatile long long out_slot[kFpRows * kFpCols];
   int rb, cb, pr;
   fp_schedule_tile(sched, blockIdx.x, rb, cb, pr);
@@ -335,7 +335,9 @@ __global__ void __launch_bounds__(kFpRows* kFpCols, 4)
   const int theta = angle0 + 2 * pr;
   if (iu >= g.cols || iv >= g.rows) return;
   const int slot = threadIdx.y * kFpRows + threadIdx.x;
-  const bool pair_in = theta + 1 < g.nangles;
+  // the launch covers angles angle0 .. angle_end - 1: an odd count leaves the
+  // last thread one angle
+  const bool pair_in = theta + 1 < angle_end;
   out_slot[slot] = (((long long)iv * g.nangles + theta) * g.cols + iu) * 2 + (pair_in ? 1 : 0);
   float ta, tb = 0.0f, Wa = 0.0f, Wb = 0.0f;
   if (pair_in)
@@ -369,11 +371,12 @@ namespace {
 // strides count elements, so both types use the same plan).
 template <typename E>
 void launch_fp_elems(const tsgb_projector* p, const float* vol, float* sino, bool additive,
-                     E* copies, cudaStream_t stream, const FpSirt* sirt) {
+                     E* copies, cudaStream_t stream, const FpSirt* sirt, int angle_begin,
+                     int angle_end, bool copies_ready) {
   const DeviceGeometry& g = p->g;
   const LayoutTable lt = make_layout_table(p);
   const long long vstride[3] = {(long long)g.ny * g.nx, (long long)g.nx, 1};
-  for (int i = 0; i < lt.count; ++i) {
+  for (int i = 0; i < lt.count && !copies_ready; ++i) {
     const Layout& L = p->layouts[i];
     if (L.b == 2) {  // b is x: a plain copy reads and writes along x
       const long long total = L.n_d * (L.n_a + 2 * kPad) * (L.n_b + 2 * kPad);
@@ -395,28 +398,33 @@ void launch_fp_elems(const tsgb_projector* p, const float* vol, float* sino, boo
   const long long per_pair = (long long)((g.rows + kFpRows - 1) / kFpRows) *
                              ((g.cols + kFpCols - 1) / kFpCols);
   const long long chunk = fp_angle_chunk(g);
-  for (long long a0 = 0; a0 < g.nangles; a0 += chunk) {
-    const int n = int(g.nangles - a0 < chunk ? g.nangles - a0 : chunk);
+  for (long long a0 = angle_begin; a0 < angle_end; a0 += chunk) {
+    const int n = int(angle_end - a0 < chunk ? angle_end - a0 : chunk);
     const FpSchedule s = fp_schedule(p, (n + 1) / 2);
     const long long blocks = per_pair * s.pairs;
     if (sirt)
       fp_ray_kernel<true, E><<<unsigned(blocks), dim3(kFpRows, kFpCols), 0, stream>>>(
-          p->d_params, p->d_columns, copies, sino, g, s, int(a0), 0, *sirt);
+          p->d_params, p->d_columns, copies, sino, g, s, int(a0), int(a0) + n, 0, *sirt);
     else
       fp_ray_kernel<false, E><<<unsigned(blocks), dim3(kFpRows, kFpCols), 0, stream>>>(
-          p->d_params, p->d_columns, copies, sino, g, s, int(a0), additive ? 1 : 0, FpSirt{});
+          p->d_params, p->d_columns, copies, sino, g, s, int(a0), int(a0) + n, additive ? 1 : 0,
+          FpSirt{});
   }
 }
 
 }  // namespace
 
 int launch_fp(const tsgb_projector* p, const float* vol, float* sino, bool additive,
-              float* workspace, void* stream_, const FpSirt* sirt) {
+              float* workspace, void* stream_, const FpSirt* sirt, int angle_begin,
+              int angle_end, bool copies_ready) {
   cudaStream_t stream = static_cast<cudaStream_t>(stream_);
+  if (angle_end < 0) angle_end = p->g.nangles;
   if (p->tuning.fp_pair_layout)
-    launch_fp_elems(p, vol, sino, additive, reinterpret_cast<float2*>(workspace), stream, sirt);
+    launch_fp_elems(p, vol, sino, additive, reinterpret_cast<float2*>(workspace), stream, sirt,
+                    angle_begin, angle_end, copies_ready);
   else
-    launch_fp_elems(p, vol, sino, additive, workspace, stream, sirt);
+    launch_fp_elems(p, vol, sino, additive, workspace, stream, sirt, angle_begin, angle_end,
+                    copies_ready);
   return int(cudaGetLastError());
 }
 

@@ -124,6 +124,8 @@ struct tsgb_projector {
   tsgb::AngleParams* d_params = nullptr;
   tsgb::ColumnEntry* d_columns = nullptr;  // [nangles][cols]
   int* d_sep_angles = nullptr;             // angle ids for the separable BP kernel
+  std::vector<int> host_sep_angles;        // the same lists on the host (angle ranges)
+  std::vector<int> host_gen_angles;
   int* d_gen_angles = nullptr;             // angle ids for the general BP kernel
   int* d_bil_fast = nullptr;               // angle ids, bilinear z-flat kernel
   int* d_bil_slow = nullptr;               // angle ids, bilinear general kernel
@@ -172,10 +174,13 @@ struct FpSirt {
 
 // Kernel launchers (fp.cu, bp.cu). All return cudaGetLastError() as int.
 // With `sirt` the forward projection writes the SIRT residual instead of sino.
+// angle_begin / angle_end: project only these angles (their sinogram slices;
+// -1 = all); copies_ready: the workspace already holds this volume's copies.
 int launch_fp(const tsgb_projector* p, const float* vol, float* sino, bool additive,
-              float* workspace, void* stream, const FpSirt* sirt = nullptr);
+              float* workspace, void* stream, const FpSirt* sirt = nullptr, int angle_begin = 0,
+              int angle_end = -1, bool copies_ready = false);
 int launch_bp_matched(const tsgb_projector* p, float* vol, const float* sino, bool additive,
-                      float* workspace, void* stream);
+                      float* workspace, void* stream, int angle_begin = 0, int angle_end = -1);
 int launch_bp_bilinear(const tsgb_projector* p, float* vol, const float* sino, bool additive,
                        float* workspace, void* stream);
 

@@ -170,6 +170,82 @@ def _as_device_tensor(arr, device, copy_in):
     return torch.empty(t.shape, dtype=torch.float32, device=device), True
 
 
+# Host data: stream the sinogram between host and device in angle chunks,
+# overlapped with the projection of the other chunks, when it is at least this
+# large (tsgb_direct_fp_angles / tsgb_direct_bp_angles / tsgb_copy_sino_angles).
+PIPELINE_MIN_BYTES = 256 << 20
+PIPELINE_CHUNKS = 8
+_copy_streams = {}
+
+
+def _host_ptr(arr):
+    return arr.ctypes.data if isinstance(arr, np.ndarray) else arr.data_ptr()
+
+
+def _pipelined(projector, forward, additive, bp_kind, src, dst):
+    """Both buffers on the host and large enough to hide their transfers."""
+    rows, nang, cols = projector.sino_shape
+    return (projector.detector_supersampling == 1 and (forward or bp_kind == "matched")
+            and 4 * rows * nang * cols >= PIPELINE_MIN_BYTES and nang >= 2 * PIPELINE_CHUNKS)
+
+
+def _project_pipelined(projector, forward, additive, src, dst, device):
+    """Host-to-host projection with the sinogram streamed in angle chunks.
+
+    Forward: the volume goes in, then chunk c is projected while chunk c - 1
+    is copied out. Backward (matched): chunk c is copied in while chunk c - 1
+    is backprojected into the volume, which then comes out. Results equal the
+    one-call path (the backprojection up to fp32 summation order).
+    """
+    lib = _native.load()
+    rows, nang, cols = projector.sino_shape
+    bounds = np.linspace(0, nang, PIPELINE_CHUNKS + 1).astype(int)
+    with torch.cuda.device(device):
+        h = projector.handle(device.index)
+        comp = torch.cuda.current_stream(device)
+        copy = _copy_streams.setdefault(device.index, torch.cuda.Stream(device))
+        nbytes = projector.workspace_bytes(device.index, forward, "matched")
+        ws = torch.empty(max(nbytes, 1), dtype=torch.uint8, device=device)
+        start = torch.cuda.Event()
+        if forward:
+            d_vol, _ = _as_device_tensor(src, device, copy_in=True)
+            d_sino, _ = _as_device_tensor(dst, device, copy_in=additive)
+            start.record(comp)
+            copy.wait_event(start)
+            for c in range(PIPELINE_CHUNKS):
+                a0, a1 = int(bounds[c]), int(bounds[c + 1])
+                _native.check(lib.tsgb_direct_fp_angles(h, d_vol.data_ptr(), d_sino.data_ptr(),
+                                                        int(bool(additive)), a0, a1, int(c > 0),
+                                                        ws.data_ptr(), nbytes, comp.cuda_stream),
+                              "tsgb_direct_fp_angles")
+                done = torch.cuda.Event()
+                done.record(comp)
+                copy.wait_event(done)
+                _native.check(lib.tsgb_copy_sino_angles(_host_ptr(dst), d_sino.data_ptr(), rows,
+                                                        nang, cols, a0, a1, copy.cuda_stream),
+                              "tsgb_copy_sino_angles")
+            copy.synchronize()
+        else:
+            d_sino = torch.empty((rows, nang, cols), dtype=torch.float32, device=device)
+            d_vol, _ = _as_device_tensor(dst, device, copy_in=additive)
+            start.record(comp)
+            copy.wait_event(start)
+            for c in range(PIPELINE_CHUNKS):
+                a0, a1 = int(bounds[c]), int(bounds[c + 1])
+                _native.check(lib.tsgb_copy_sino_angles(d_sino.data_ptr(), _host_ptr(src), rows,
+                                                        nang, cols, a0, a1, copy.cuda_stream),
+                              "tsgb_copy_sino_angles")
+                arrived = torch.cuda.Event()
+                arrived.record(copy)
+                comp.wait_event(arrived)
+                _native.check(lib.tsgb_direct_bp_angles(h, d_vol.data_ptr(), d_sino.data_ptr(),
+                                                        int(bool(additive) or c > 0), a0, a1,
+                                                        ws.data_ptr(), nbytes, comp.cuda_stream),
+                              "tsgb_direct_bp_angles")
+            target = torch.from_numpy(dst) if isinstance(dst, np.ndarray) else dst
+            target.copy_(d_vol)
+
+
 def direct_project(projector, vol_link, proj_link, forward=None, additive=False,
                    bp_kind="matched"):
     """Forward (``forward=True``) or back project between two links."""
@@ -196,6 +272,8 @@ def direct_project(projector, vol_link, proj_link, forward=None, additive=False,
     on_gpu = isinstance(vol, torch.Tensor) and vol.is_cuda
     device = vol.device if on_gpu else _cuda_device_for_host_data()
     src, dst = (vol, sino) if forward else (sino, vol)
+    if not on_gpu and _pipelined(projector, forward, additive, bp_kind, src, dst):
+        return _project_pipelined(projector, forward, additive, src, dst, device)
     d_src, _ = _as_device_tensor(src, device, copy_in=True)
     d_dst, copy_back = _as_device_tensor(dst, device, copy_in=additive)
     lib = _native.load()
