@@ -506,7 +506,7 @@ def run_ours(args, rank, world, local_rank):
         xh = x.cpu().pin_memory()
         yh = torch.empty(A.range_shape, dtype=torch.float32).pin_memory()
         vh = torch.empty(A.domain_shape, dtype=torch.float32).pin_memory()
-        for _ in range(max(1, args.warmup // 2)):
+        for _ in range(max(1, args.warmup)):
             A(xh, out=yh)
             A.T(yh, out=vh)
         torch.cuda.synchronize()
