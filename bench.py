@@ -241,7 +241,7 @@ def noisy_projection(torch, A, x, seed):
 def bench_batched_sirt(torch, ts, device, n_jobs=64, iterations=30, seed=3):
     """64 independent jobs (64^3..256^3, parallel or cone, 60-720 angles, detector
     side x 1.5 side, noisy data): batched SIRT vs looping the plain operator."""
-    from tomosipo_gb300.sirt import BatchedSirt, sirt
+    from tomosipo_gb300.sirt import BatchedSirt, autotune_jobs, sirt
 
     rng = np.random.default_rng(seed)
     jobs, updates = [], 0
@@ -257,6 +257,11 @@ def bench_batched_sirt(torch, ts, device, n_jobs=64, iterations=30, seed=3):
         jobs.append((A, y))
         updates += 2 * n ** 3 * angles * iterations
     torch.cuda.synchronize()
+    # forward schedules from the autotuner, one run per job shape (timed apart);
+    # both paths below use them
+    t0 = time.perf_counter()
+    tuning = autotune_jobs([j[0] for j in jobs], device)
+    t_tune = time.perf_counter() - t0
     # warm both paths once on the smallest job
     small = min(jobs, key=lambda j: j[1].numel())
     sirt(small[0], small[1], 1)
@@ -276,12 +281,15 @@ def bench_batched_sirt(torch, ts, device, n_jobs=64, iterations=30, seed=3):
     return {
         "config": f"{n_jobs} jobs, sides from {{64,96,128,192,256}}, parallel/cone 50/50, "
                   f"60-720 angles, {iterations} iterations, y = A(x) + N(0, 0.01 max) (seed {seed}); "
-                  "times include computing R and C",
+                  "forward schedules from the autotuner (one run per job shape, timed apart "
+                  "as autotune_s); times include computing R and C",
         "solves_per_s": n_jobs / t_batch,
         "plain_loop_solves_per_s": n_jobs / t_plain,
         "speedup_vs_plain_loop": t_plain / t_batch,
         "batched_s": t_batch,
         "plain_loop_s": t_plain,
+        "autotune_s": t_tune,
+        "autotuned_shapes": len(tuning),
         "gups": updates / t_batch / 1e9,
     }
 

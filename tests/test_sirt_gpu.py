@@ -120,3 +120,15 @@ def test_server_results_same_alone_and_in_mix(dev):
 
 def r_iters(reqs, rid):
     return next(q.iterations for q in reqs if q.id == rid)
+
+
+def test_autotuned_batch_equals_plain(dev):
+    """Autotuned forward schedules (one autotuner run per job shape) change the
+    order of independent tiles only: the batch still equals the plain loop."""
+    jobs = [_job(dev, 24, True, 30, 31), _job(dev, 24, True, 36, 32), _job(dev, 32, False, 20, 33)]
+    b = BatchedSirt([(A, y) for A, y, _ in jobs], autotune=True)
+    assert len(b.tuning) == 2  # two shapes: 24^3 cone (twice) and 32^3 parallel
+    b.run(3, graph=False)
+    for (A, y, _), xb in zip(jobs, b.x):
+        assert torch.equal(xb, sirt(A, y, 3))
+    b.close()

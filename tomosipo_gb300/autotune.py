@@ -65,15 +65,25 @@ def _time_fp(A, x, y, repeats):
     return start.elapsed_time(end) / repeats
 
 
-def autotune(A, device=None, repeats=None, cache_path=None, verbose=False):
+def shape_key(projector):
+    """Key of a projector's sizes and beam kind only (angles and vectors ignored):
+    operators that share it take the same schedule well."""
+    return "vol{}_det{}x{}_k{}".format(
+        "x".join(map(str, projector.vol_shape)), projector.sino_shape[0],
+        projector.sino_shape[2], int(projector.proj_desc.kind))
+
+
+def autotune(A, device=None, repeats=None, cache_path=None, verbose=False, key=None):
     """Pick the fastest forward schedule for operator ``A`` and set it.
 
-    Returns ``{"tuning": {...}, "ms": best time, "default_ms": time of the
-    starting schedule, "trials": n, "cached": bool}``.
+    ``key``: cache key (default: ``geometry_key``, the exact geometry; pass
+    ``shape_key(A.projector)`` to share results between operators of the same
+    sizes). Returns ``{"tuning": {...}, "ms": best time, "default_ms": time of
+    the starting schedule, "trials": n, "cached": bool}``.
     """
     proj = A.projector
     dev = torch.device("cuda", torch.cuda.current_device() if device is None else device)
-    key = geometry_key(proj)
+    key = key or geometry_key(proj)
     hit = _cache.get(key)
     if hit is None and cache_path and os.path.exists(cache_path):
         hit = _load_file(cache_path).get(key)

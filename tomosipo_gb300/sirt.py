@@ -84,6 +84,23 @@ class SirtJobState:
         return 2 * vol + 4 * sino + 32 * angles * cols + stats_ws
 
 
+def autotune_jobs(operators, device):
+    """Autotune the forward schedules of many operators: one autotuner run per
+    (volume shape, detector shape, beam kind), its schedule set on every
+    operator of that shape (the batch launches each job's forward projection in
+    its projector's schedule). Returns {shape key: tuning}."""
+    from .autotune import autotune, shape_key
+
+    tuning = {}
+    with torch.cuda.device(device):
+        for A in operators:
+            key = shape_key(A.projector)
+            if key not in tuning:
+                tuning[key] = autotune(A, device.index, key=key)["tuning"]
+            A.projector.set_tuning(device.index, **tuning[key])
+    return tuning
+
+
 class NativeBatch:
     """Native job table over a list of SirtJobState (rebuilt when jobs change)."""
 
@@ -140,7 +157,9 @@ class BatchedSirt:
 
     ``jobs`` is a list of ``(A, y)`` or ``(A, y, x_init)`` with ``y`` a CUDA
     tensor on one device; jobs may differ in size and geometry (their
-    detectors' v axis must run along z: circular and helical scans).
+    detectors' v axis must run along z: circular and helical scans). With
+    ``autotune`` the forward schedules come from the autotuner, one run per
+    job shape (``tomosipo_gb300.autotune``; results are cached per shape).
     ``run(n, graph=True)`` captures ``graph_iterations`` iterations of all jobs
     in one CUDA graph (a job's next iteration need not wait for the other
     jobs) and replays it. ``x[i]`` is job i's reconstruction, equal to
@@ -149,12 +168,13 @@ class BatchedSirt:
 
     graph_iterations = 10
 
-    def __init__(self, jobs):
+    def __init__(self, jobs, autotune=False):
         if not jobs:
             raise ValueError("BatchedSirt needs at least one job")
         self.device = jobs[0][1].device
         if self.device.type != "cuda":
             raise ValueError("BatchedSirt runs on CUDA tensors")
+        self.tuning = autotune_jobs([j[0] for j in jobs], self.device) if autotune else {}
         self.states = [SirtJobState(j[0], j[1], j[2] if len(j) > 2 else None, self.device)
                        for j in jobs]
         self._native = NativeBatch(self.states)
