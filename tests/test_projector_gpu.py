@@ -221,3 +221,39 @@ def test_wide_sinogram_paths_by_linearity(device):
     assert rel_l2(bb.cpu().numpy(), bb_split.cpu().numpy()) <= TOL_ORACLE
     del y, bp, bb
     torch.cuda.empty_cache()
+
+
+BP_EDGE_CASES = {
+    # detector columns ~4x finer than voxels: many columns reach each voxel
+    "fine_columns": (ts.volume(shape=(20, 24, 40), size=(0.5, 0.6, 1.0)),
+                     ts.cone(angles=10, shape=(20, 240), size=(0.7, 1.6), cone_angle=0.3)),
+    # detector rows ~3x finer than voxels along z: several rows per voxel
+    # (the backprojector's row-loop path)
+    "fine_rows": (ts.volume(shape=24, size=1),
+                  ts.parallel(angles=12, shape=(80, 36), size=(1.2, 1.5))),
+    # a detector shorter than the volume: rows clamped into the padding
+    "tall_volume": (ts.volume(shape=(150, 20, 36), size=(3.0, 0.4, 0.72)),
+                    ts.cone(angles=9, shape=(40, 50), size=(1.2, 1.0), src_orig_dist=3,
+                            src_det_dist=4)),
+}
+
+
+@pytest.mark.parametrize("name", sorted(BP_EDGE_CASES))
+def test_matched_bp_edge_geometries(name, device):
+    """Matched backprojection against the oracle where detector sampling is
+    much finer than the voxels (along u or v) or the detector is shorter than
+    the volume, with adjointness and the additive form."""
+    vg, pg = BP_EDGE_CASES[name]
+    A = ts.operator(vg, pg)
+    x = noise_cube_phantom(vg.shape, seed=21)
+    y_gpu = A(torch.from_numpy(x).to(device)).cpu().numpy()
+    assert rel_l2(y_gpu, orc.fp(vg, pg, x)) <= TOL_ORACLE
+    yy = np.random.default_rng(22).random(A.range_shape).astype(np.float32)
+    yt = torch.from_numpy(yy).to(device)
+    x_ref = orc.bp_matched(vg, pg, yy)
+    xb = A.T(yt)
+    assert rel_l2(xb.cpu().numpy(), x_ref) <= TOL_ORACLE, rel_l2(xb.cpu().numpy(), x_ref)
+    assert adjoint_error(y_gpu, yy, x, xb.cpu().numpy()) <= TOL_ADJOINT
+    acc = xb.clone()
+    ts.operator(vg, pg, additive=True).T(yt, out=acc)
+    assert rel_l2(acc.cpu().numpy(), 2 * x_ref) <= TOL_ORACLE
