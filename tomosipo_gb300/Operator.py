@@ -48,7 +48,16 @@ def to_astra_compatible_operator_geometry(vg, pg):
 
 def operator(volume_geometry, projection_geometry, voxel_supersampling=1,
              detector_supersampling=1, additive=False, backprojector="matched"):
-    """Create a new tomographic operator."""
+    """Create a new tomographic operator (``tomosipo/Operator.py:63-106``).
+
+    ``detector_supersampling`` d: the forward projection averages d x d rays
+    per detector pixel, and the matched backprojection is its exact
+    transpose. ``voxel_supersampling`` d: the bilinear backprojection
+    (``backprojector="bilinear"``, ASTRA's voxel-driven kind) averages d^3
+    points per voxel. The matched backprojection (the default) is the exact
+    transpose of the forward projection, which samples rays and not voxels,
+    so voxel supersampling does not change it.
+    """
     return Operator(
         volume_geometry,
         projection_geometry,
