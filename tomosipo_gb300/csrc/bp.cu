@@ -139,7 +139,7 @@ __device__ __forceinline__ void bp_sep_accumulate(const AngleParams* __restrict_
       bool any = false;
 #pragma unroll
       for (int m = 0; m < kA; ++m) {
-        h[m] = fmaxf(0.0f, 1.0f - fabsf(qa - float(m)));
+        h[m] = __saturatef(1.0f - fabsf(qa - float(m)));
         any = any || h[m] > 0.0f;
       }
       if (!any) continue;
@@ -153,7 +153,9 @@ __device__ __forceinline__ void bp_sep_accumulate(const AngleParams* __restrict_
         // Voxel j's row position vs = (z_j - B) / Sl; row v0's ray passes the
         // plane at t0 = q_b - z_j = v0 Sl + (B - zt0) - j = -Sl (vs - v0), and
         // row v0+1's at t0 + Sl, so |t0 + Sl| = |Sl| - |t0| for the rows the
-        // run selects: tent(t0 + Sl) = max(0, 1 - |Sl| + |t0|).
+        // run selects: tent(t0 + Sl) = max(0, 1 - |Sl| + |t0|). Both tents are
+        // at most 1 (|t0| >= 0, |t0| < |Sl|), so clamping to [0, 1] is the same
+        // max(0, .) and fuses into the add.
         const float vs0 = (zt0 - B) * inv;
         const float vs1 = fmaf(float(kRun - 1), inv, vs0);
         const float C0 = B - zt0;
@@ -172,7 +174,7 @@ __device__ __forceinline__ void bp_sep_accumulate(const AngleParams* __restrict_
             const float v0 = floorf(fmaf(float(j), inv, vs0));
             const float at0 = fabsf(fmaf(v0, Sl, C0) - float(j));
             const float2 yy = __ldg(colv + Offset((int)v0) * rs);
-            const float V = fmaf(fmaxf(0.0f, 1.0f - at0), yy.x, fmaxf(0.0f, c1s + at0) * yy.y);
+            const float V = fmaf(__saturatef(1.0f - at0), yy.x, __saturatef(c1s + at0) * yy.y);
 #pragma unroll
             for (int m = 0; m < kA; ++m) acc[m][j] = fmaf(h[m], V, acc[m][j]);
           }
@@ -182,7 +184,7 @@ __device__ __forceinline__ void bp_sep_accumulate(const AngleParams* __restrict_
             const float v0 = fminf(fmaxf(floorf(fmaf(float(j), inv, vs0)), vmin), vmax);
             const float at0 = fabsf(fmaf(v0, Sl, C0) - float(j));
             const float2 yy = __ldg(colv + Offset((int)v0) * rs);
-            const float V = fmaf(fmaxf(0.0f, 1.0f - at0), yy.x, fmaxf(0.0f, c1s + at0) * yy.y);
+            const float V = fmaf(__saturatef(1.0f - at0), yy.x, __saturatef(c1s + at0) * yy.y);
 #pragma unroll
             for (int m = 0; m < kA; ++m) acc[m][j] = fmaf(h[m], V, acc[m][j]);
           }
