@@ -81,6 +81,14 @@ __global__ void __launch_bounds__(256)
   out[((long long)iv * g.nangles + theta) * g.cols + iu] = make_float2(a, b);
 }
 
+// Element `row` rows below `col`, rows `rs_bytes` bytes apart: a signed
+// 32 x 32 -> 64-bit product (int) or a 64-bit one (long long).
+template <typename Offset>
+__device__ __forceinline__ const float2* row_at(const float2* col, int row, Offset rs_bytes) {
+  return reinterpret_cast<const float2*>(reinterpret_cast<const char*>(col) +
+                                         (long long)row * (long long)rs_bytes);
+}
+
 // Matched backprojection of separable angles (det_v along z, so b = z) that
 // share their in-plane axis a, for kA voxel columns adjacent along a (at
 // a-coordinates it0 .. it0 + kA - 1, all on the plane kt of the dominant axis
@@ -97,8 +105,9 @@ __global__ void __launch_bounds__(256)
 // sinow is the row-pair weighted sinogram (bp_weight_kernel) with kRowPad
 // padding rows above and below the detector (rows -kRowPad .. rows + kRowPad
 // - 1), so the two-row path reads both rows with one load and without bounds
-// tests once its row index is clamped into the padding. Offsets (in pairs)
-// are 32-bit unless kWide (padded sinogram of 2^31 pairs or more).
+// tests once its row index is clamped into the padding. Offsets are 32-bit
+// unless kWide (padded sinogram of 2^31 pairs or more, or rows 2^31 bytes or
+// more apart).
 template <int kA, int kRun, bool kWide>
 __device__ __forceinline__ void bp_sep_accumulate(const AngleParams* __restrict__ params,
                                                   const ColumnEntry* __restrict__ columns,
@@ -109,6 +118,9 @@ __device__ __forceinline__ void bp_sep_accumulate(const AngleParams* __restrict_
   using Offset = typename std::conditional<kWide, long long, int>::type;
   const float zt0 = float(z0 - g.oz);
   const Offset rs = Offset(g.nangles) * g.cols;  // row stride
+  // row stride in bytes; below 2^31 unless kWide, so a row's address is one
+  // 32 x 32 -> 64-bit multiply-add
+  const Offset rs_bytes = rs * Offset(sizeof(float2));
   const float2* __restrict__ sinow0 = sinow + (long long)kRowPad * rs;  // row 0
   const float vmin = float(-kRowPad - g.ov), vmax = float(g.rows - g.ov);
   const float4* __restrict__ col4 = reinterpret_cast<const float4*>(columns);
@@ -173,7 +185,7 @@ __device__ __forceinline__ void bp_sep_accumulate(const AngleParams* __restrict_
           for (int j = 0; j < kRun; ++j) {
             const float v0 = floorf(fmaf(float(j), inv, vs0));
             const float at0 = fabsf(fmaf(v0, Sl, C0) - float(j));
-            const float2 yy = __ldg(colv + Offset((int)v0) * rs);
+            const float2 yy = __ldg(row_at(colv, (int)v0, rs_bytes));
             const float V = fmaf(__saturatef(1.0f - at0), yy.x, __saturatef(c1s + at0) * yy.y);
 #pragma unroll
             for (int m = 0; m < kA; ++m) acc[m][j] = fmaf(h[m], V, acc[m][j]);
@@ -183,7 +195,7 @@ __device__ __forceinline__ void bp_sep_accumulate(const AngleParams* __restrict_
           for (int j = 0; j < kRun; ++j) {
             const float v0 = fminf(fmaxf(floorf(fmaf(float(j), inv, vs0)), vmin), vmax);
             const float at0 = fabsf(fmaf(v0, Sl, C0) - float(j));
-            const float2 yy = __ldg(colv + Offset((int)v0) * rs);
+            const float2 yy = __ldg(row_at(colv, (int)v0, rs_bytes));
             const float V = fmaf(__saturatef(1.0f - at0), yy.x, __saturatef(c1s + at0) * yy.y);
 #pragma unroll
             for (int m = 0; m < kA; ++m) acc[m][j] = fmaf(h[m], V, acc[m][j]);
@@ -463,13 +475,15 @@ __global__ void bp_bilinear_prep_kernel(const float* __restrict__ sino, float4* 
 // floor(vt) of the column (clamped into the zero padding when `clamp`),
 // interpolated, times the weight (for cone beams K times the source distance).
 template <bool kCone>
-__device__ __forceinline__ float bilinear_z_term(const float4* __restrict__ colq, int rs, float vt,
+__device__ __forceinline__ float bilinear_z_term(const float4* __restrict__ colq, int rs_bytes,
+                                                 float vt,
                                                  float vmin, float vmax, bool clamp, float fu,
                                                  float K, float dz, float dxy2, float acc) {
   float fv0 = floorf(vt);
   const float fv = vt - fv0;
   if (clamp) fv0 = fminf(fmaxf(fv0, vmin), vmax);  // rows outside read the zero padding
-  const float4 q = __ldg(colq + (int)fv0 * rs);
+  const float4 q = __ldg(reinterpret_cast<const float4*>(reinterpret_cast<const char*>(colq) +
+                                                       (long long)(int)fv0 * rs_bytes));
   const float top = fmaf(fu, q.y - q.x, q.x);
   const float bot = fmaf(fu, q.w - q.z, q.z);
   const float val = fmaf(fv, bot - top, top);
@@ -500,6 +514,7 @@ __global__ void __launch_bounds__(kBpX* kBpY)
   const float xt = float(x - g.ox), yt = float(y - g.oy), zt0 = float(z0 - g.oz);
   const int cp = g.cols + 2 * kColPad;
   const int rs = g.nangles * cp;  // padded row stride (padded copy < 2^31 quads)
+  const int rs_bytes = rs * int(sizeof(float4));  // < 2^31 (the plan checks it)
   const float4* __restrict__ base0 = sinoq + kRowPad * rs + kColPad;
   const float umin = float(-kColPad - g.ou), umax = float(g.cols - g.ou);
   const float vmin = float(-kRowPad - g.ov), vmax = float(g.rows - g.ov);
@@ -537,13 +552,15 @@ __global__ void __launch_bounds__(kBpX* kBpY)
     if (inside) {
 #pragma unroll
       for (int j = 0; j < kRun; ++j)
-        acc[j] = bilinear_z_term<kCone>(colq, rs, fmaf(float(j), dv, vt0), vmin, vmax, false, fu,
-                                        K, fmaf(float(j), g.vs[0], dz0), dxy2, acc[j]);
+        acc[j] = bilinear_z_term<kCone>(colq, rs_bytes, fmaf(float(j), dv, vt0), vmin, vmax,
+                                        false, fu, K, fmaf(float(j), g.vs[0], dz0), dxy2,
+                                        acc[j]);
     } else {
 #pragma unroll
       for (int j = 0; j < kRun; ++j)
-        acc[j] = bilinear_z_term<kCone>(colq, rs, fmaf(float(j), dv, vt0), vmin, vmax, true, fu,
-                                        K, fmaf(float(j), g.vs[0], dz0), dxy2, acc[j]);
+        acc[j] = bilinear_z_term<kCone>(colq, rs_bytes, fmaf(float(j), dv, vt0), vmin, vmax,
+                                        true, fu, K, fmaf(float(j), g.vs[0], dz0), dxy2,
+                                        acc[j]);
     }
   }
 #pragma unroll
@@ -600,7 +617,11 @@ void launch_sep_pass(const tsgb_projector* p, bool a_is_x, const int* angles, in
                      const float2* pairs, float* vol, const float* C, float* scratch,
                      cudaStream_t stream) {
   const DeviceGeometry& g = p->g;
-  const bool wide = (size_t)(g.rows + 2 * kRowPad) * g.nangles * g.cols >= (size_t(1) << 31);
+  // 32-bit offsets need fewer than 2^31 padded pairs and a row stride below
+  // 2^31 bytes
+  const size_t rs = (size_t)g.nangles * g.cols;
+  const bool wide = (size_t)(g.rows + 2 * kRowPad) * rs >= (size_t(1) << 31) ||
+                    rs * sizeof(float2) >= (size_t(1) << 31);
   if (wide && a_is_x)
     launch_sep_pass_m<true, true>(p, angles, n, mode, pairs, vol, C, scratch, stream);
   else if (wide)

@@ -231,8 +231,11 @@ std::string build_plan(const tsgb_volume_desc* vol, const tsgb_projection_desc* 
     }
     // Exact zeros when det_v runs along z (V = (v, 0, 0)): then u and the
     // projective denominator are constant along a voxel column in z.
-    const bool pad_fits = int64_t(g.rows + 2 * kRowPad) * g.nangles * (g.cols + 2 * kColPad) <
-                          (int64_t(1) << 31);
+    // the z-flat kernel's quad copy needs 32-bit offsets: fewer than 2^31
+    // quads, rows fewer than 2^31 bytes apart
+    const int64_t quad_row = int64_t(g.nangles) * (g.cols + 2 * kColPad);
+    const bool pad_fits = int64_t(g.rows + 2 * kRowPad) * quad_row < (int64_t(1) << 31) &&
+                          quad_row * 16 < (int64_t(1) << 31);
     ap.bil_zflat = (pad_fits && voxel_ss == 1 && pu[0] == 0.0 && pw[0] == 0.0) ? 1 : 0;
     (ap.bil_zflat ? bil_fast : bil_slow)->push_back(t);
     for (int i = 0; i < 3; ++i) ap.src[i] = float(S[i]);
