@@ -168,9 +168,9 @@ __device__ __forceinline__ void bp_sep_accumulate(const AngleParams* __restrict_
         // run selects: tent(t0 + Sl) = max(0, 1 - |Sl| + |t0|). Both tents are
         // at most 1 (|t0| >= 0, |t0| < |Sl|), so clamping to [0, 1] is the same
         // max(0, .) and fuses into the add.
-        const float vs0 = (zt0 - B) * inv;
-        const float vs1 = fmaf(float(kRun - 1), inv, vs0);
         const float C0 = B - zt0;
+        const float vs0 = -C0 * inv;  // (zt0 - B) * inv: IEEE subtraction is antisymmetric
+        const float vs1 = fmaf(float(kRun - 1), inv, vs0);
         const float c1s = 1.0f - fabsf(Sl);
         const float2* __restrict__ colv = col + Offset(g.ov) * rs;  // row 0 of this column
         // vs is monotone in j: if both ends select rows inside [vmin, vmax]
