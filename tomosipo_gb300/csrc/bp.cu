@@ -47,38 +47,48 @@ constexpr int kRunZ = kBpRunZ;      // voxels along z per thread (matched)
 constexpr int kRunZBil = 8;         // voxels along z per thread (bilinear)
 
 // W * y of pixel (iv, iu) at angle theta (0 for rows outside the detector and
-// for rays the forward projector does not sample).
-__device__ __forceinline__ float weighted_pixel(const AngleParams& ap,
-                                                const ColumnEntry* __restrict__ columns,
+// for rays the forward projector does not sample). ce is the pixel's column
+// entry (read only for separable angles).
+__device__ __forceinline__ float weighted_pixel(const AngleParams& ap, const ColumnEntry& ce,
                                                 const float* __restrict__ sino,
                                                 const DeviceGeometry& g, int iv, int iu,
                                                 int theta) {
   if (iv < 0 || iv >= g.rows) return 0.0f;
   const float vt = float(iv - g.ov);
-  const Ray r = ap.separable ? ray_column(columns[(size_t)theta * g.cols + iu], vt)
-                             : ray_general(ap, float(iu - g.ou), vt);
+  const Ray r = ap.separable ? ray_column(ce, vt) : ray_general(ap, float(iu - g.ou), vt);
   float w = 0.0f;
   if (finite_ray(r) && fabsf(r.ma) <= kMaxSlope && fabsf(r.mb) <= kMaxSlope) w = ray_step(ap, r);
   return w * __ldg(sino + ((size_t)iv * g.nangles + theta) * g.cols + iu);
 }
 
 // Row-pair weighted sinogram: element (iv, theta, iu) holds (W y[iv], W y[iv+1])
-// for iv = -1 .. rows-1 (blockIdx.y / threadIdx.y count from iv = -1), so one
-// 8-byte load gives the backprojector both rows of a tap. Elements iv = -2,
-// rows and rows+1 (the padding) are zeroed by the caller. `out` points at
-// element (0, 0, 0); rows are nangles * cols elements apart.
+// for iv = -1 .. rows-1, so one 8-byte load gives the backprojector both rows
+// of a tap. A thread walks kWeightRows consecutive pair rows of one detector
+// column (threadIdx.y / blockIdx.y count them from iv = -1), loading the
+// column's entry once and computing each row's W y once: the row's value is
+// the second of one pair and the first of the next. Elements iv = -2, rows and
+// rows+1 (the padding) are zeroed by the caller. `out` points at element
+// (0, 0, 0); rows are nangles * cols elements apart.
+constexpr int kWeightRows = 8;
+
 __global__ void __launch_bounds__(256)
     bp_weight_kernel(const AngleParams* __restrict__ params,
                      const ColumnEntry* __restrict__ columns, const float* __restrict__ sino,
                      float2* __restrict__ out, DeviceGeometry g) {
   const int iu = blockIdx.x * 32 + threadIdx.x;
-  const int iv = blockIdx.y * 8 + threadIdx.y - 1;
+  const int r0 = (blockIdx.y * 8 + threadIdx.y) * kWeightRows - 1;
   const int theta = blockIdx.z;
-  if (iu >= g.cols || iv >= g.rows) return;
+  if (iu >= g.cols || r0 >= g.rows) return;
   const AngleParams& ap = params[theta];
-  const float a = weighted_pixel(ap, columns, sino, g, iv, iu, theta);
-  const float b = weighted_pixel(ap, columns, sino, g, iv + 1, iu, theta);
-  out[((long long)iv * g.nangles + theta) * g.cols + iu] = make_float2(a, b);
+  ColumnEntry ce{};
+  if (ap.separable) ce = columns[(size_t)theta * g.cols + iu];
+  float prev = weighted_pixel(ap, ce, sino, g, r0, iu, theta);
+  const int r1 = min(r0 + kWeightRows, g.rows);
+  for (int iv = r0; iv < r1; ++iv) {
+    const float next = weighted_pixel(ap, ce, sino, g, iv + 1, iu, theta);
+    out[((long long)iv * g.nangles + theta) * g.cols + iu] = make_float2(prev, next);
+    prev = next;
+  }
 }
 
 // Element `row` rows below `col`, rows `rs_bytes` bytes apart: a signed
@@ -686,7 +696,8 @@ int launch_bp_matched(const tsgb_projector* p, float* vol, const float* sino, bo
     const dim3 block(32, 8);
     for (int a0 = angle_begin; a0 < angle_end; a0 += 65535) {
       const int n = angle_end - a0 < 65535 ? angle_end - a0 : 65535;
-      const dim3 grid((g.cols + 31) / 32, (g.rows + 1 + 7) / 8, n);
+      const dim3 grid((g.cols + 31) / 32, (g.rows + 1 + 8 * kWeightRows - 1) / (8 * kWeightRows),
+                      n);
       // offset the angle through the pointers: rows are strided by nangles*cols
       bp_weight_kernel<<<grid, block, 0, stream>>>(p->d_params + a0, p->d_columns + (size_t)a0 * g.cols,
                                                    sino + (size_t)a0 * g.cols,
