@@ -169,3 +169,11 @@ def test_volume_vec_with_operator_normalisation():
     vg2, pg2 = to_astra_compatible_operator_geometry(T * R * vg.to_vec(), T * R * pg)
     assert vg2 == ts.volume(shape=(8, 9, 10), size=(1, 1.5, 2))
     assert pg2 == pg
+
+
+def test_hollow_box_phantom_mean():
+    """tomosipo's only numeric known answer for the phantom
+    (``tests/test_phantom.py:11-17``): a 100^3 hollow box has mean 0.208."""
+    vd = ts.data(ts.volume(shape=100))
+    ts.phantom.hollow_box(vd)
+    assert vd.data.mean() == pytest.approx(0.208)

@@ -16,6 +16,7 @@ import numpy as np
 
 from . import vector_calc as vc
 from .geometry import VolumeGeometry, VolumeVectorGeometry, volume, from_perspective
+from .Data import Data, data
 from .links.base import link, geometry_shape
 from .projector import create_projector, direct_fp, direct_bp, BP_KINDS
 
@@ -69,6 +70,10 @@ def operator(volume_geometry, projection_geometry, voxel_supersampling=1,
 
 
 def _to_link(geometry, x):
+    """A dataset's own link, or a new link around an array
+    (``tomosipo/Operator.py:109-113``)."""
+    if isinstance(x, Data):
+        return x.link
     return link(geometry, x)
 
 
@@ -106,6 +111,8 @@ class Operator:
         else:
             plink = vlink.new_empty(self.range_shape)
         direct_fp(self.projector, vlink, plink, additive=self.additive)
+        if isinstance(volume, Data):  # a dataset in, a dataset out (tomosipo/Operator.py:189-192)
+            return data(self.projection_geometry, plink.data)
         return plink.data
 
     def _bp(self, projection, out=None):
@@ -118,6 +125,8 @@ class Operator:
             vlink = plink.new_empty(self.domain_shape)
         direct_bp(self.projector, vlink, plink, additive=self.additive,
                   bp_kind=self.backprojector)
+        if isinstance(projection, Data):  # tomosipo/Operator.py:230-233
+            return data(self.volume_geometry, vlink.data)
         return vlink.data
 
     def __call__(self, volume, out=None):
