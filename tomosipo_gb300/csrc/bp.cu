@@ -626,7 +626,7 @@ void launch_sep_tile(const tsgb_projector* p, const int* angles, int n, const fl
 template <bool kWide, bool kAisX, int kMode>
 void launch_sep_pass_t(const tsgb_projector* p, const int* angles, int n, const float2* pairs,
                        float* vol, const float* C, float* scratch, cudaStream_t stream) {
-  if (kAisX)
+  if constexpr (kAisX)
     launch_sep_tile<kWide, kAisX, kMode, 8, false>(p, angles, n, pairs, vol, C, scratch, stream);
   else
     launch_sep_tile<kWide, kAisX, kMode, 4, true>(p, angles, n, pairs, vol, C, scratch, stream);
