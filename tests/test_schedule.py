@@ -9,6 +9,7 @@ schedule gives bit-identical sinograms.
 """
 import itertools
 
+import numpy as np
 import pytest
 
 
@@ -43,3 +44,22 @@ def test_patch_tiles_are_contiguous():
     assert {s[1] for s in seen} == set(range(16))
     assert {s[2] for s in seen} == set(range(8))
     assert seen[:3] == [(0, 0, 0), (1, 0, 0), (2, 0, 0)]
+
+
+@pytest.mark.parametrize("nang", [16, 17, 40, 100, 360, 1024, 4097])
+def test_pipeline_chunk_bounds(nang):
+    """Angle chunks of a streamed projection cover every angle once, in order;
+    the chunk whose transfer is exposed (the backprojection's first, the
+    forward projection's last) is the smallest, and the rest grow by at most
+    PIPELINE_GROWTH from it."""
+    from tomosipo_gb300.projector import PIPELINE_GROWTH, _chunk_bounds
+
+    for forward in (False, True):
+        b = [int(v) for v in _chunk_bounds(nang, forward)]
+        sizes = np.diff(b)
+        assert b[0] == 0 and b[-1] == nang and np.all(sizes >= 1)
+        grow = sizes if not forward else sizes[::-1]
+        assert grow[0] == min(sizes) <= max(1, nang // 32)
+        assert np.all(grow[1:] <= grow[:-1] * PIPELINE_GROWTH)
+    assert list(_chunk_bounds(1024, False)) == [0, 32, 288, 1024]
+    assert list(_chunk_bounds(1024, True)) == [0, 736, 992, 1024]
