@@ -461,6 +461,8 @@ def run_ours(args, rank, world, local_rank):
     torch.cuda.set_device(device)
     vg, pg = workload_geometry(ts)
     A = ts.operator(vg, pg)
+    if args.fp_copies != "auto":
+        A.projector.set_tuning(device.index, fp_pair_layout=int(args.fp_copies == "pairs"))
     x = phantom_gpu(torch, device, N, count=20, seed=2)
     y = torch.empty(A.range_shape, device=device)
     v = torch.empty(A.domain_shape, device=device)
@@ -592,7 +594,8 @@ def run_ours(args, rank, world, local_rank):
         "vs_baseline": None,
         "dtype": "f32",
         "data": "synthetic",
-        "config": config({"parallelism": f"replicas x{world}" if world > 1 else "single GPU"}),
+        "config": config(dict({"parallelism": f"replicas x{world}" if world > 1 else "single GPU"},
+                              **({"fp_copies": args.fp_copies} if args.fp_copies != "auto" else {}))),
         "fp_ms": statistics.mean(fp_ms),
         "bp_ms": statistics.mean(bp_ms),
         "roofline": {
@@ -636,6 +639,10 @@ def main():
     p.add_argument("--serve-requests", type=int, default=8)
     p.add_argument("--workload", choices=sorted(WORKLOADS), default="headline",
                    help="headline = the metric's 512^3/1024 workload; c2 = 256^3/360 (profiling)")
+    p.add_argument("--fp-copies", choices=["auto", "single", "pairs"], default="auto",
+                   help="forward projector's volume copies (tuning fp_pair_layout; auto = the "
+                   "projector's default): to profile the headline's single-voxel copies on "
+                   "the c2 workload")
     args = p.parse_args()
     global N, ANGLES, DET
     N, ANGLES, DET = WORKLOADS[args.workload]
