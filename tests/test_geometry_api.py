@@ -1,0 +1,227 @@
+"""Geometry API behaviour that tomosipo's own geometry tests pin
+(``tests/geometry/test_parallel.py``, ``test_cone.py``, ``test_volume.py``,
+``test_concatenate.py``), restated with seeded inputs: indexing rules, corners,
+reshaping and rescaling, ASTRA round trips, transforms (with the warning when a
+non-vector geometry becomes a vector one), ``project_point`` relations,
+``to_vol``, volume operations and ``ts.concatenate``. Host only.
+"""
+import numpy as np
+import pytest
+
+import tomosipo_gb300 as ts
+from tomosipo_gb300 import vector_calc as vc
+from tomosipo_gb300.geometry import (
+    random_cone,
+    random_cone_vec,
+    random_parallel,
+    random_parallel_vec,
+    random_transform,
+    random_volume,
+    random_volume_vec,
+)
+from tomosipo_gb300.geometry import transform
+
+
+@pytest.fixture(autouse=True)
+def _seeded():
+    np.random.seed(123)  # the random_* helpers draw from NumPy's global generator
+
+
+def _par_geoms():
+    np.random.seed(7)
+    return [ts.parallel(angles=2), ts.parallel(angles=10, size=3, shape=11),
+            ts.parallel(angles=5, size=7, shape=23), random_parallel(), random_parallel()]
+
+
+def _cone_geoms():
+    np.random.seed(8)
+    return [ts.cone(angles=3, cone_angle=0.5), ts.cone(angles=12, shape=(6, 10), size=(1.5, 2.5),
+                                                      src_orig_dist=4, src_det_dist=6),
+            random_cone(), random_cone()]
+
+
+# ------------------------------------------------------------------ indexing
+def test_parallel_getitem_rules():
+    pg = ts.parallel(angles=10, shape=20)
+    assert pg[1].num_angles == pg[:1].num_angles == pg[-1].num_angles == 1
+    assert pg[:2].num_angles == 2 and pg[:].num_angles == 10
+    assert pg[-1] == pg[9] and pg[-2] == pg[8]
+    assert pg[np.ones(pg.num_angles) == 1] == pg
+    assert pg[np.arange(pg.num_angles) % 2 == 0] == pg[0::2]
+    with pytest.raises(ValueError):
+        pg[:, 0, 0]  # no detector indexing on a non-vector geometry
+    with pytest.raises(IndexError):
+        ts.parallel(angles=3)[4]
+    for g in _par_geoms():
+        assert g == g[:]
+        with pytest.raises(ValueError):
+            g[:, :]
+        assert g[1::2].num_angles == g.num_angles // 2
+        assert g[1:9:2].angles == pytest.approx(g.angles[1:9:2])
+        assert g[-1].angles == pytest.approx(g.angles[-1:])
+        assert g[-2].angles == pytest.approx(g.angles[-2:-1])
+
+
+def test_cone_getitem_rules():
+    pg = ts.cone(angles=10, shape=20, cone_angle=0.5)
+    assert pg[3].num_angles == 1 and pg[-1] == pg[9]
+    assert pg[np.arange(10) % 3 == 0] == pg[0::3]
+    with pytest.raises(ValueError):
+        pg[:, 0, 0]
+
+
+# ---------------------------------------------------------------- properties
+@pytest.mark.parametrize("kind", ["parallel", "cone"])
+def test_det_properties_and_corners(kind):
+    for pg in (_par_geoms() if kind == "parallel" else _cone_geoms()):
+        n = pg.num_angles
+        for name in ("det_pos", "det_v", "det_u", "det_normal"):
+            assert getattr(pg, name).shape == (n, 3), name
+        assert pg.det_sizes.shape == (n, 2) and pg.corners.shape == (n, 4, 3)
+        assert pg.lower_left_corner == pytest.approx(pg.corners[:, 0, :])
+        half = pg.det_shape[0] * pg.det_v / 2 + pg.det_shape[1] * pg.det_u / 2
+        assert pg.det_pos - pg.lower_left_corner == pytest.approx(half)
+        assert pg.det_shape == pg.to_vec().det_shape and pg.num_angles == pg.to_vec().num_angles
+        assert pg.det_sizes == pytest.approx(pg.to_vec().det_sizes)
+        assert pg.det_pos == pytest.approx(pg.to_vol().pos)
+
+
+def test_parallel_has_no_source():
+    for pg in _par_geoms():
+        assert pg.ray_dir.shape == (pg.num_angles, 3)
+        with pytest.raises(NotImplementedError):
+            pg.src_pos
+
+
+def test_cone_distances_and_sizes():
+    assert ts.cone(size=np.sqrt(2), src_orig_dist=5.0).src_orig_dist == 5.0
+    assert ts.cone(size=np.sqrt(2), src_det_dist=3.0).src_det_dist == 3.0
+    pg = ts.cone(angles=3, cone_angle=0.5, size=(1, 2))
+    assert np.abs(pg.det_sizes - np.array([[1, 2]])).sum() < ts.epsilon
+
+
+# -------------------------------------------------------- reshape and rescale
+def test_reshape_keeps_detector_size():
+    for pg in _par_geoms() + _cone_geoms():
+        assert pg.reshape(1).det_shape == (1, 1)
+        assert pg.reshape((3, 5)).det_shape == (3, 5)
+        assert pg.reshape((3, 5)).det_sizes == pytest.approx(pg.det_sizes)
+
+
+def test_rescale_det():
+    for pg in _par_geoms():
+        if pg.det_shape[0] % 2 == 0 and pg.det_shape[1] % 2 == 0:
+            r = pg.rescale_det(2)
+            assert r.angles == pytest.approx(pg.angles)
+            assert r.det_shape == (pg.det_shape[0] // 2, pg.det_shape[1] // 2)
+            assert r.det_sizes == pytest.approx(pg.det_sizes)
+            assert r.det_v == pytest.approx(2 * pg.det_v)
+            assert r.det_u == pytest.approx(2 * pg.det_u)
+    pg = ts.cone(size=np.sqrt(2), cone_angle=0.5, angles=10, shape=20)
+    assert pg.rescale_det(2).det_sizes == pytest.approx(pg.det_sizes)
+    assert pg.rescale_det((2, 2)) == pg.rescale_det(2)
+    assert pg.rescale_det(10).det_shape == (2, 2)
+
+
+# ------------------------------------------------------------- ASTRA round trip
+def test_astra_round_trips():
+    for pg in _par_geoms() + _cone_geoms():
+        assert pg == ts.from_astra(pg.to_astra())
+        assert ts.from_astra(pg.to_vec().to_astra()) == ts.from_astra(pg.to_astra()).to_vec()
+    rng = np.random.default_rng(9)
+    for _ in range(20):
+        n = int(rng.integers(1, 100))
+        angles = rng.uniform(0, 2 * np.pi, n) if rng.random() < 0.5 else n
+        pg = ts.cone(angles=angles, shape=rng.integers(1, 100, size=2), size=rng.uniform(1, 100, 2),
+                     cone_angle=rng.uniform(0.5, 1))
+        assert pg == ts.from_astra(pg.to_astra())
+
+
+# ----------------------------------------------------------------- transforms
+def test_transforms_compose_and_convert_with_a_warning():
+    for pg in _par_geoms()[:3] + _cone_geoms()[:3]:
+        T1, T2 = random_transform(), random_transform()
+        with pytest.warns(UserWarning):
+            assert (T1 * T2) * pg == T1 * (T2 * pg)
+        with pytest.warns(UserWarning):
+            assert transform.identity() * pg == pg.to_vec()
+    for pg in (random_parallel_vec(), random_cone_vec()):
+        T = random_transform()
+        assert T.inv * (T * pg) == pg
+
+
+def test_parallel_project_point_relations():
+    p = vc.to_vec((3, 5, 7))
+    for pg in _par_geoms():
+        assert pg.project_point(pg.det_pos) == pytest.approx(np.zeros((pg.num_angles, 2)))
+        with pytest.warns(UserWarning):
+            moved = ts.translate(pg.ray_dir) * pg  # along the rays: same projection
+        assert pg.project_point(p) == pytest.approx(moved.project_point(p))
+        with pytest.warns(UserWarning):
+            moved = ts.translate(pg.det_normal) * pg
+        assert pg.project_point(p) == pytest.approx(moved.project_point(p))
+        with pytest.warns(UserWarning):
+            moved = ts.translate(pg.det_v + pg.det_u) * pg  # one pixel along v and u
+        assert pg.project_point(p) - moved.project_point(p) == pytest.approx(
+            np.ones((pg.num_angles, 2)))
+
+
+def test_cone_project_point_of_detector_centre():
+    for pg in _cone_geoms():
+        assert pg.project_point(pg.det_pos) == pytest.approx(np.zeros((pg.num_angles, 2)),
+                                                            abs=1e-9)
+
+
+# -------------------------------------------------------------------- volumes
+def test_volume_operations():
+    vg = ts.volume()
+    t = (5, 5, 5)
+    assert vg in vg and vg in vg.scale(2)
+    assert vg not in vg.translate(t) and vg not in vg.scale(0.5)
+    assert vg.translate(t) in vg.translate(t).scale(2)
+    assert vg.reshape(100) == vg.reshape((100,) * 3)
+    v3 = ts.volume(shape=(3, 5, 7))
+    assert np.allclose(v3.to_vec().size, v3.size)
+    v10 = ts.volume(shape=10, size=10, pos=0)
+    assert v10.with_voxel_size(1.0) == v10
+    assert v10.with_voxel_size(2.0) == ts.volume(shape=5, size=10, pos=0)
+    assert v10.with_voxel_size(3.0) == v10.with_voxel_size((3.0, 3.0, 3.0))
+
+
+# ---------------------------------------------------------------- concatenate
+def test_concatenate_transforms():
+    t = random_transform()
+    tt = ts.concatenate([t, t])
+    assert tt.num_steps == 2 * t.num_steps and tt[: t.num_steps] == t
+
+
+@pytest.mark.parametrize("make", [random_cone, random_cone_vec, random_parallel,
+                                  random_parallel_vec, random_volume, random_volume_vec])
+def test_concatenate_geometries(make):
+    g = make()
+    gg = ts.concatenate([g, g])
+    assert gg.num_steps == 2 * g.num_steps
+    assert gg[: g.num_steps] == g.to_vec() and gg[g.num_steps:] == g.to_vec()
+
+
+def test_concatenate_errors():
+    with pytest.raises(TypeError):
+        ts.concatenate(ts.volume())  # not a sequence
+    with pytest.raises(TypeError):
+        ts.concatenate([ts.volume(), ts.parallel()])
+    with pytest.raises(ValueError):
+        ts.concatenate([])
+    with pytest.raises(ValueError):
+        ts.concatenate([ts.parallel(shape=3), ts.parallel(shape=4)])
+    with pytest.raises(ValueError):
+        ts.concatenate([ts.volume(shape=3), ts.volume(shape=4)])
+
+
+def test_concatenated_scans_project_as_one():
+    """Two half scans joined by concatenate describe the same rays as the full
+    scan: their vectors match the full geometry's, angle for angle."""
+    full = ts.cone(angles=8, shape=(4, 6), size=(1, 1.5), src_orig_dist=3, src_det_dist=5)
+    joined = ts.concatenate([full[:4], full[4:]])
+    v = full.to_vec()
+    for name in ("src_pos", "det_pos", "det_v", "det_u"):
+        assert getattr(joined, name) == pytest.approx(getattr(v, name))

@@ -3,8 +3,8 @@
 ``import tomosipo_gb300 as ts`` gives the names tomosipo exports for the
 projection path (``tomosipo/__init__.py:10-41``): ``operator``, ``data``,
 ``volume``, ``volume_vec``, ``parallel``, ``parallel_vec``, ``cone``,
-``cone_vec``, the transforms, ``link``, ``to_astra`` / ``from_astra`` and
-``epsilon``; ``tomosipo_gb300.astra`` has the legacy ``forward``/``backward``
+``cone_vec``, the transforms, ``concatenate``, ``link``, ``to_astra`` /
+``from_astra`` and ``epsilon``; ``tomosipo_gb300.astra`` has the legacy ``forward``/``backward``
 and ``fdk``.
 """
 __version__ = "0.6.0+gb300"
@@ -26,6 +26,7 @@ from .geometry.transform import (
     to_perspective,
     from_perspective,
 )
+from .geometry.concatenate import concatenate
 from .links.base import link
 from . import links
 from . import phantom

@@ -18,6 +18,7 @@ from .transform import (
 )
 from .volume import VolumeGeometry, volume, is_volume, random_volume
 from .volume_vec import VolumeVectorGeometry, volume_vec, random_volume_vec
+from .concatenate import concatenate
 
 
 def from_astra_projection_geometry(astra_pg):
