@@ -225,3 +225,18 @@ def test_concatenated_scans_project_as_one():
     v = full.to_vec()
     for name in ("src_pos", "det_pos", "det_v", "det_u"):
         assert getattr(joined, name) == pytest.approx(getattr(v, name))
+
+
+def test_det_vec_astra_round_trip_and_conversion_module():
+    """The detector-only geometry converts to tomosipo's ``det_vec`` pseudo-type
+    and back, through ``ts.from_astra`` and the ``ts.geometry.conversion`` name."""
+    from tomosipo_gb300.geometry import random_det_vec
+
+    for _ in range(5):
+        g = random_det_vec()
+        d = g.to_astra()
+        assert d["type"] == "det_vec" and d["Vectors"].shape == (g.num_angles, 12)
+        assert ts.from_astra(d) == g
+        assert ts.geometry.conversion.from_astra_projection_geometry(d) == g
+    with pytest.raises(ValueError):
+        ts.geometry.conversion.from_astra_projection_geometry({"type": "fanflat"})

@@ -19,16 +19,5 @@ from .transform import (
 from .volume import VolumeGeometry, volume, is_volume, random_volume
 from .volume_vec import VolumeVectorGeometry, volume_vec, random_volume_vec
 from .concatenate import concatenate
-
-
-def from_astra_projection_geometry(astra_pg):
-    kinds = {
-        "parallel3d": ParallelGeometry,
-        "parallel3d_vec": ParallelVectorGeometry,
-        "cone": ConeGeometry,
-        "cone_vec": ConeVectorGeometry,
-    }
-    kind = astra_pg.get("type")
-    if kind not in kinds:
-        raise ValueError(f"ASTRA projection geometry type {kind!r} is not supported.")
-    return kinds[kind].from_astra(astra_pg)
+from . import conversion
+from .conversion import from_astra_projection_geometry

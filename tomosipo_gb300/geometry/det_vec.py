@@ -110,6 +110,32 @@ class DetectorVectorGeometry(ProjectionGeometry):
             u=self._det_u,
         )
 
+    def to_astra(self):
+        """ASTRA-style dict of the detector alone (tomosipo's ``det_vec`` pseudo-type,
+        ``tomosipo/geometry/det_vec.py:180-199``): the vector rows of a
+        ``*_vec`` geometry with zeros where the source or ray direction goes."""
+        rows, cols = self.det_shape
+        return {
+            "type": "det_vec",
+            "DetectorRowCount": rows,
+            "DetectorColCount": cols,
+            "Vectors": self._astra_vectors(np.zeros_like(self._det_pos)),
+        }
+
+    @staticmethod
+    def from_astra(astra_pg):
+        if astra_pg["type"] != "det_vec":
+            raise ValueError(
+                "DetectorVectorGeometry.from_astra only supports 'det_vec' type astra geometries."
+            )
+        vec = np.asarray(astra_pg["Vectors"], dtype=np.float64)
+        return det_vec(
+            (astra_pg["DetectorRowCount"], astra_pg["DetectorColCount"]),
+            det_pos=vec[:, 3:6][:, ::-1],
+            det_v=vec[:, 9:12][:, ::-1],
+            det_u=vec[:, 6:9][:, ::-1],
+        )
+
     def _astra_vectors(self, first):
         return np.concatenate(
             [first[:, ::-1], self._det_pos[:, ::-1], self._det_u[:, ::-1], self._det_v[:, ::-1]],
