@@ -27,6 +27,9 @@ def test_accepts_only_interface_objects():
     assert not CudaArrayLink.__accepts__(np.zeros(3))
     assert not CudaArrayLink.__accepts__(torch.zeros(3))
     import tomosipo_gb300.cupy  # noqa: F401  (the reference's import still works)
+    from tomosipo_gb300.links.cupy import CupyLink  # and its link module's name
+
+    assert CupyLink is CudaArrayLink
 
 
 @pytest.mark.gpu
