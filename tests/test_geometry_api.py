@@ -240,3 +240,46 @@ def test_det_vec_astra_round_trip_and_conversion_module():
         assert ts.geometry.conversion.from_astra_projection_geometry(d) == g
     with pytest.raises(ValueError):
         ts.geometry.conversion.from_astra_projection_geometry({"type": "fanflat"})
+
+
+# ------------------------------------------------------- detector-only vectors
+def _det_vecs():
+    from tomosipo_gb300.geometry import random_det_vec
+
+    np.random.seed(11)
+    return [ts.geometry.det_vec(shape=(4, 6), det_pos=np.zeros((8, 3)), det_v=(1, 0, 0),
+                                det_u=(0, 0, 1))] + [random_det_vec() for _ in range(4)]
+
+
+def test_det_vec_slicing_bins_the_detector():
+    for pg in _det_vecs():
+        assert pg == pg[:] == pg[:, :] == pg[:, :, :]
+        assert pg[1::2].num_angles == pg.num_angles // 2
+        if pg.num_angles % 2 or pg.det_shape[0] % 2 or pg.det_shape[1] % 2:
+            continue
+        assert pg[:, ::2].det_v == pytest.approx(2 * pg.det_v)
+        assert pg[:, :, ::2].det_u == pytest.approx(2 * pg.det_u)
+        assert pg[:, ::2].det_pos != pytest.approx(pg[:, 1::2].det_pos)
+        assert pg[:, ::2, :].det_sizes == pytest.approx(pg[:, 1::2, :].det_sizes)
+        assert pg[:, :, ::2].det_sizes == pytest.approx(pg[:, :, 1::2].det_sizes)
+
+
+def test_det_vec_properties_and_transforms():
+    for pg in _det_vecs():
+        assert pg == pg.to_vec()
+        assert pg.det_pos == pytest.approx(pg.to_vol().pos)
+        with pytest.raises(NotImplementedError):
+            pg.src_pos
+        with pytest.raises(NotImplementedError):
+            pg.ray_dir
+        with pytest.raises(NotImplementedError):
+            pg.project_point((0, 0, 0))
+        assert pg.corners.shape == (pg.num_angles, 4, 3)
+        assert pg.lower_left_corner == pytest.approx(pg.corners[:, 0, :])
+        T1, T2 = random_transform(), random_transform()
+        assert (T1 * T2) * pg == T1 * (T2 * pg)
+        assert transform.identity() * pg == pg
+        if pg.det_shape[0] % 2 == 0 and pg.det_shape[1] % 2 == 0:
+            assert pg.rescale_det(2).det_v == pytest.approx(2 * pg.det_v)
+    unit = ts.geometry.det_vec(shape=1, det_pos=(0, 0, 0), det_v=(1, 0, 0), det_u=(0, 0, 1))
+    assert unit.det_normal == pytest.approx(np.array([(0, 1, 0)]))

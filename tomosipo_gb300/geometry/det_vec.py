@@ -210,6 +210,11 @@ class DetectorVectorGeometry(ProjectionGeometry):
             self._det_u * self.det_shape[1] / new_shape[1],
         )
 
+    def project_point(self, point):
+        """A detector alone has no source or ray direction to project along
+        (tomosipo raises the same)."""
+        raise NotImplementedError()
+
     def _project(self, origin, direction):
         point = types.to_vec(origin)
         hit = vc.intersect(point, direction, self._det_pos, self.det_normal)
