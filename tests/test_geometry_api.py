@@ -283,3 +283,69 @@ def test_det_vec_properties_and_transforms():
             assert pg.rescale_det(2).det_v == pytest.approx(2 * pg.det_v)
     unit = ts.geometry.det_vec(shape=1, det_pos=(0, 0, 0), det_v=(1, 0, 0), det_u=(0, 0, 1))
     assert unit.det_normal == pytest.approx(np.array([(0, 1, 0)]))
+
+
+# ------------------------------------------------------------- volume vectors
+def test_volume_vec_init_and_repr():
+    z, y, x = (1, 0, 0), (0, 1, 0), (0, 0, 1)
+    ob = ts.volume_vec(shape=1, pos=0, w=z, v=y, u=x)
+    assert ob == ts.volume_vec(shape=1, pos=0, w=z, v=y)
+    assert ob == ts.volume_vec(shape=1, pos=0, w=[z], v=y)
+    assert ob == ts.volume_vec(shape=(1, 1, 1), pos=[(0, 0, 0)], w=z, v=y, u=x)
+    n = 11
+    for bad in (dict(pos=[(0, 0, 0)] * 3, w=[z] * n, v=[y] * n, u=[x] * n),
+                dict(pos=[(0, 0, 0)] * n, w=[z] * 3, v=[y] * n, u=[x] * n),
+                dict(pos=[(0, 0, 0)] * n, w=[z] * n, v=[y] * 3, u=[x] * n),
+                dict(pos=[(0, 0, 0)] * n, w=[z] * n, v=[y] * n, u=[x] * 3)):
+        with pytest.raises(ValueError):
+            ts.volume_vec(shape=1, **bad)
+    unit_box = ts.volume_vec(shape=1, pos=(0, 0, 0))
+    expected = """ts.volume_vec(
+    shape=(1, 1, 1),
+    pos=array([[0., 0., 0.]]),
+    w=array([[1., 0., 0.]]),
+    v=array([[0., 1., 0.]]),
+    u=array([[0., 0., 1.]]),
+)"""
+    assert repr(unit_box) == expected
+    with np.printoptions(legacy="1.13"):
+        assert repr(unit_box) == expected
+    for vg in (random_volume_vec(), ts.volume(shape=(3, 5, 7)).to_vec()):
+        assert eval(repr(vg), dict(ts=ts, array=np.array)) == vg
+
+
+def test_volume_vec_indexing_and_transforms():
+    vg = random_volume_vec()
+    assert vg[0] == vg[:1] == vg[-1] == vg[:] == vg
+    assert ts.concatenate([vg, vg])[0] == vg and ts.concatenate([vg, vg])[1] == vg
+    assert vg[np.ones(len(vg)) == 1] == vg
+    assert vg[np.arange(len(vg)) % 2 == 0] == vg[0::2]
+    assert ts.volume_vec(shape=3)[:, 1, 1, 1] == ts.volume_vec(shape=1)
+    T = random_transform()
+    assert T * vg[:, 1, 2, 3] == (T * vg)[:, 1, 2, 3]
+    assert T * vg[:, :1, :2, :3] == (T * vg)[:, :1, :2, :3]
+    assert T * vg[:, 1:, 2:, 3:] == (T * vg)[:, 1:, 2:, 3:]
+    with pytest.raises(ValueError):
+        vg[1, 2, 3, 4, 5]
+    Tt = ts.translate(np.random.normal(size=3))
+    assert (Tt * vg).w == pytest.approx(vg.w) and (Tt * vg).u == pytest.approx(vg.u)
+    assert (Tt * vg).size == vg.size and (Tt * vg).voxel_size == vg.voxel_size
+    S = ts.scale(abs(np.random.normal(size=(3, 3))))  # different scaling at each step and axis
+    with pytest.raises(ValueError):
+        (S * random_volume().to_vec()).size
+
+
+def test_volume_vec_corners():
+    zero, z, y, x = (0, 0, 0), (1, 0, 0), (0, 1, 0), (0, 0, 1)
+    n = 11
+    vg = ts.volume_vec(shape=1, pos=[zero] * n, w=[z] * n, v=[y] * n, u=[x] * n)
+    assert vg.corners.shape == (n, 8, 3)
+    assert np.allclose(ts.volume_vec(shape=1, pos=0).lower_left_corner, [(-0.5,) * 3])
+    assert np.allclose(ts.volume_vec(shape=1, pos=(0.5,) * 3).lower_left_corner, [(0,) * 3])
+    frame = dict(w=(2, 3, 5), v=(7, 11, 13), u=(17, 19, 23))
+    small = ts.volume_vec(shape=(1, 2, 3), pos=zero, **frame)
+    big = ts.volume_vec(shape=(2, 4, 6), pos=zero, **frame)
+    assert np.abs(small.corners * 2.0 - big.corners).sum() == pytest.approx(0.0)
+    moved = ts.volume_vec(shape=(1, 2, 3), pos=(5, 7, 11), w=z, v=y, u=x)
+    base = ts.volume_vec(shape=(1, 2, 3), pos=zero, w=z, v=y, u=x)
+    assert np.abs((moved.corners - base.corners) - (5, 7, 11)).sum() == pytest.approx(0.0)
