@@ -349,3 +349,70 @@ def test_volume_vec_corners():
     moved = ts.volume_vec(shape=(1, 2, 3), pos=(5, 7, 11), w=z, v=y, u=x)
     base = ts.volume_vec(shape=(1, 2, 3), pos=zero, w=z, v=y, u=x)
     assert np.abs((moved.corners - base.corners) - (5, 7, 11)).sum() == pytest.approx(0.0)
+
+
+# ---------------------------------------------------------- vector geometries
+def test_parallel_vec_init_validation_repr_and_equality():
+    vecs = np.arange(30).reshape((10, 3))
+    kw = dict(ray_dir=vecs, det_pos=vecs, det_v=vecs, det_u=vecs)
+    assert ts.parallel_vec(shape=1, **kw).det_shape == (1, 1)
+    assert ts.parallel_vec(shape=(3, 5), **kw).det_shape == (3, 5)
+    with pytest.raises(TypeError):
+        ts.parallel_vec(1, **kw)  # shape is keyword-only
+    with pytest.raises(TypeError):
+        ts.parallel_vec(shape=0, **kw)
+    with pytest.raises(TypeError):
+        two = np.random.normal(size=(10, 2))
+        ts.parallel_vec(shape=1, ray_dir=two, det_pos=two, det_v=two, det_u=two)
+    with pytest.raises(ValueError):
+        ts.parallel_vec(shape=1, ray_dir=np.random.normal(size=(10, 3)),
+                        det_pos=np.random.normal(size=(11, 3)),
+                        det_v=np.random.normal(size=(12, 3)), det_u=np.random.normal(size=(13, 3)))
+    x = [[1, 2, 3], [4, 5, 6]]
+    pg = ts.parallel_vec(shape=10, ray_dir=x, det_pos=x, det_v=x, det_u=x)
+    expected = """ts.parallel_vec(
+    shape=(10, 10),
+    ray_dir=array([[1., 2., 3.],
+       [4., 5., 6.]]),
+    det_pos=array([[1., 2., 3.],
+       [4., 5., 6.]]),
+    det_v=array([[1., 2., 3.],
+       [4., 5., 6.]]),
+    det_u=array([[1., 2., 3.],
+       [4., 5., 6.]]),
+)"""
+    assert repr(pg) == expected
+    with np.printoptions(legacy="1.13"):
+        assert repr(pg) == expected
+    r = random_parallel()
+    assert eval(repr(r), dict(ts=ts, array=np.array)) == r
+    z = np.array([(0, 0, 0)])
+    pg = ts.parallel_vec(shape=10, ray_dir=z, det_pos=z, det_v=z, det_u=z)
+    unequal = [ts.parallel_vec(shape=9, ray_dir=z, det_pos=z, det_v=z, det_u=z),
+               ts.parallel_vec(shape=10, ray_dir=z + 1, det_pos=z, det_v=z, det_u=z),
+               ts.parallel_vec(shape=10, ray_dir=z, det_pos=z + 1, det_v=z, det_u=z),
+               ts.parallel_vec(shape=10, ray_dir=z, det_pos=z, det_v=z + 1, det_u=z),
+               ts.parallel_vec(shape=10, ray_dir=z, det_pos=z, det_v=z, det_u=z + 1),
+               ts.cone(size=np.sqrt(2), cone_angle=0.5, angles=2),
+               ts.cone(size=np.sqrt(2), cone_angle=0.5).to_vec(), ts.volume()]
+    assert pg == pg
+    for u in unequal:
+        assert u != pg and pg != u
+
+
+@pytest.mark.parametrize("make", [random_parallel_vec, random_cone_vec])
+def test_vector_geometry_slicing(make):
+    for _ in range(4):
+        pg = make()
+        assert pg == pg[:] == pg[:, :] == pg[:, :, :]
+        assert pg[np.ones(pg.num_angles) == 1] == pg
+        assert pg[np.arange(pg.num_angles) % 2 == 0] == pg[0::2]
+        assert pg[1::2].num_angles == pg.num_angles // 2
+        assert pg[1:9:2].det_pos == pytest.approx(pg.det_pos[1:9:2, :])
+        assert pg[-1].det_pos == pytest.approx(pg.det_pos[-1:, :])
+        if pg.num_angles % 2 or pg.det_shape[0] % 2 or pg.det_shape[1] % 2:
+            continue
+        assert pg[:, ::2].det_v == pytest.approx(2 * pg.det_v)
+        assert pg[:, :, ::2].det_u == pytest.approx(2 * pg.det_u)
+        assert pg[:, ::2].det_pos != pytest.approx(pg[:, 1::2].det_pos)
+        assert pg[:, ::2, :].det_sizes == pytest.approx(pg[:, 1::2, :].det_sizes)

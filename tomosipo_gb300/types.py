@@ -10,6 +10,8 @@ from numbers import Integral
 
 import numpy as np
 
+EPSILON = 1e-8  # the package's ts.epsilon (tomosipo/__init__.py:41)
+
 
 def _as_tuple(val, n):
     if isinstance(val, abc.Iterable) and not isinstance(val, (str, bytes)):
@@ -38,8 +40,8 @@ def _to_shape(shape, n):
             out.append(int(s))
         else:
             raise TypeError(f"Shape must contain only integers. Got {shape}.")
-    if any(s < 0 for s in out):
-        raise ValueError(f"Shape must be non-negative. Got {shape}.")
+    if any(s < 1 for s in out):  # tomosipo/types.py:111-126: a TypeError, as for non-integers
+        raise TypeError(f"Shape must be positive. Got {tuple(out)}.")
     return tuple(out)
 
 
@@ -55,8 +57,8 @@ def to_shape3d(shape):
 
 def _to_size(size, n):
     size = to_float_tuple(size, n, "size")
-    if any(s < 0 for s in size):
-        raise ValueError(f"Size must be non-negative. Got {size}.")
+    if any(s < -EPSILON for s in size):  # tomosipo/types.py:160-170
+        raise TypeError(f"Size must be non-negative. Got {size}.")
     return size
 
 
