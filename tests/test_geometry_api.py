@@ -416,3 +416,56 @@ def test_vector_geometry_slicing(make):
         assert pg[:, :, ::2].det_u == pytest.approx(2 * pg.det_u)
         assert pg[:, ::2].det_pos != pytest.approx(pg[:, 1::2].det_pos)
         assert pg[:, ::2, :].det_sizes == pytest.approx(pg[:, 1::2, :].det_sizes)
+
+
+# ------------------------------------------------------------- plain volumes
+def test_volume_pos_size_extent():
+    from tomosipo_gb300.geometry.volume import _extent_to_pos_size, _pos_size_to_extent
+
+    for _ in range(10):
+        pos, size = np.random.normal(size=3), np.square(np.random.normal(size=3))
+        p2, s2 = _extent_to_pos_size(_pos_size_to_extent(pos, size))
+        assert np.allclose(p2, pos) and np.allclose(s2, size)
+    assert ts.geometry.is_volume(ts.volume()) and ts.geometry.is_volume(ts.volume().to_vec())
+    assert not ts.geometry.is_volume(ts.cone(cone_angle=0.5)) and not ts.geometry.is_volume(None)
+    assert ts.volume().shape == (1, 1, 1) and ts.volume(shape=(3, 4, 5)).shape == (3, 4, 5)
+    extent = ((0, 1), (3, 4), (5, 6))
+    assert ts.volume(extent=extent).extent == extent
+    assert ts.volume(pos=(0.5, 0.5, 0.5), size=1).extent == ((0, 1),) * 3
+    # pos and size, or extent, not both
+    for kw in (dict(pos=0, size=1, extent=extent), dict(pos=0, extent=extent),
+               dict(size=1, extent=extent)):
+        with pytest.raises(ValueError):
+            ts.volume(**kw)
+    for kw in (dict(pos=0, size=1), dict(pos=0), dict(size=1), dict(extent=extent), dict()):
+        ts.volume(**kw)
+    for bad in ((1, 0), 3):
+        with pytest.raises(TypeError):
+            ts.volume(extent=bad)
+    with pytest.raises(TypeError):
+        ts.volume(shape=0)
+
+
+def test_volume_equality_repr_and_indexing():
+    vg = ts.volume()
+    for u in (ts.volume(shape=10), ts.volume(shape=(10, 9, 8)), ts.cone(cone_angle=0.5)):
+        assert vg != u
+    box = ts.volume(shape=(1, 2, 3), pos=(4, 5, 6), size=(7, 8, 9))
+    assert repr(box) == """ts.volume(
+    shape=(1, 2, 3),
+    pos=(4.0, 5.0, 6.0),
+    size=(7.0, 8.0, 9.0),
+)"""
+    r = random_volume()
+    assert eval(repr(r), dict(ts=ts)) == r
+    assert len(ts.volume()) == 1
+    moved = ts.volume().scale((1, 2, 3)).translate((10, 20, 30))
+    assert ts.from_astra(moved.to_astra()) == moved
+    vg = ts.volume(shape=(3, 4, 5), extent=((11, 13), (17, 19), (23, 29)))
+    assert vg == vg[:, :, :] == vg[:, :] == vg[:]
+    assert vg[0, 0, 0] == vg[:1, :1, :1] and vg[0] == vg[0, :, :] and vg[-1] == vg[2]
+    assert vg[::3, ::4, ::5].shape == (1, 1, 1)
+    assert np.allclose(vg[0, 1, 2].size, np.array(vg.size) / vg.shape)  # voxel size kept
+    assert np.allclose(vg.size[1], vg[:, ::2, :].size[1])
+    assert vg.shape[1] == 2 * vg[:, ::2].shape[1]
+    assert np.allclose(vg[:, ::2, :].size, vg[:, 1::2, :].size)

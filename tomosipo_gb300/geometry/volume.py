@@ -25,11 +25,14 @@ def _pos_size_to_extent(pos, size):
 
 
 def _extent_to_pos_size(extent):
-    extent = np.array(extent, dtype=np.float64)
-    if extent.shape == (2,):
-        extent = np.broadcast_to(extent, (3, 2))
+    # three (low, high) pairs, one per axis; anything else is a TypeError, as in
+    # tomosipo/geometry/volume.py:154-158
+    try:
+        extent = np.array(extent, dtype=np.float64)
+    except (TypeError, ValueError):
+        raise TypeError(f"Expected an extent of three (low, high) pairs. Got {extent!r}.")
     if extent.shape != (3, 2):
-        raise ValueError(f"Expected extent of shape (2,) or (3, 2). Got {extent.shape}.")
+        raise TypeError(f"Expected an extent of three (low, high) pairs. Got shape {extent.shape}.")
     size = types.to_size3d(tuple(extent[:, 1] - extent[:, 0]))
     pos = types.to_pos(tuple((extent[:, 1] + extent[:, 0]) / 2))
     return pos, size
