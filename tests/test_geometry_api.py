@@ -469,3 +469,68 @@ def test_volume_equality_repr_and_indexing():
     assert np.allclose(vg.size[1], vg[:, ::2, :].size[1])
     assert vg.shape[1] == 2 * vg[:, ::2].shape[1]
     assert np.allclose(vg[:, ::2, :].size, vg[:, 1::2, :].size)
+
+
+# ------------------------------------------------- constructors, repr, equality
+def test_cone_constructor_rules():
+    with pytest.raises(TypeError):
+        ts.cone(angles=1, shape=None, cone_angle=1)
+    with pytest.raises(TypeError):
+        ts.cone(angles=None, shape=1, cone_angle=1)
+    kw = dict(angles=1, shape=1, size=1)
+    # cone_angle alone, or distances without it; not both, not neither
+    for bad in (dict(cone_angle=1, src_orig_dist=1, src_det_dist=1),
+                dict(cone_angle=1, src_orig_dist=1), dict(cone_angle=1, src_det_dist=1), dict()):
+        with pytest.raises(ValueError):
+            ts.cone(**kw, **bad)
+    for ok in (dict(cone_angle=1), dict(src_orig_dist=1, src_det_dist=1),
+               dict(src_orig_dist=1), dict(src_det_dist=1)):
+        ts.cone(**kw, **ok)
+    assert ts.cone(shape=2, cone_angle=1).det_size == (2, 2)  # size defaults to shape
+    assert ts.cone(shape=2, size=1, cone_angle=1).det_size == (1, 1)
+    assert isinstance(ts.cone(cone_angle=1), ts.geometry.ProjectionGeometry)
+    assert ts.cone(angles=np.linspace(0, 1, 100), cone_angle=1).num_angles == 100
+    with pytest.raises(TypeError):
+        ts.cone(size=np.sqrt(2), cone_angle=0.5, angles=[])
+
+
+def test_parallel_constructor_rules():
+    assert ts.parallel(angles=1, shape=1).det_shape == (1, 1)
+    assert ts.parallel(angles=1, size=1).det_sizes == pytest.approx(np.ones((1, 2)))
+    assert ts.parallel(shape=(2, 3)).det_size == (2, 3) and ts.parallel().det_shape == (1, 1)
+    assert ts.parallel(angles=10) == ts.parallel(angles=np.linspace(0, np.pi, 10, endpoint=False))
+    for bad in (dict(shape=0), dict(angles=0), dict(angles=np.ones((1, 1)))):
+        with pytest.raises(TypeError):
+            ts.parallel(**bad)
+
+
+def test_cone_and_parallel_repr_and_equality():
+    pg = ts.cone(angles=10, shape=11, size=1, src_orig_dist=5, src_det_dist=6)
+    expected = """ts.cone(
+    angles=10,
+    shape=(11, 11),
+    size=(1.0, 1.0),
+    src_orig_dist=5.0,
+    src_det_dist=6.0,
+)"""
+    assert repr(pg) == expected
+    with np.printoptions(legacy="1.13"):
+        assert repr(pg) == expected
+    pg = ts.parallel(angles=10, shape=11, size=1)
+    assert repr(pg) == """ts.parallel(
+    angles=10,
+    shape=(11, 11),
+    size=(1.0, 1.0),
+)"""
+    for make in (random_cone, random_parallel):
+        g = make()
+        assert eval(repr(g), dict(ts=ts, array=np.array)) == g
+    cg = ts.cone(size=np.sqrt(2), cone_angle=0.5)
+    for u in (ts.cone(size=5, cone_angle=0.5), ts.cone(angles=2, size=np.sqrt(2), cone_angle=0.5),
+              ts.cone(shape=2, size=np.sqrt(2), cone_angle=0.5),
+              ts.cone(size=np.sqrt(2), src_orig_dist=50), ts.cone(size=np.sqrt(2), src_det_dist=50),
+              ts.volume()):
+        assert cg != u
+    par = ts.parallel()
+    for u in (ts.parallel(angles=2), ts.parallel(size=5), ts.parallel(shape=3), ts.volume()):
+        assert u != par and par != u

@@ -74,7 +74,9 @@ class ConeGeometry(ProjectionGeometry):
         if np.isscalar(angles) and isinstance(angles, (int, np.integer)) and not isinstance(angles, bool):
             angles = np.linspace(0, 2 * np.pi, int(angles), endpoint=False)
         else:
-            angles = types.to_scalars(angles, var_name="angles", accept_empty=True)
+            # an empty array is a TypeError here, an angle count of 0 a ValueError
+            # below (tomosipo/geometry/cone.py:163-173)
+            angles = types.to_scalars(angles, var_name="angles")
         if len(angles) == 0:
             raise ValueError(
                 f"ConeGeometry expects non-empty array of angles; got {self.angles_original}"
