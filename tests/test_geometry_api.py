@@ -534,3 +534,51 @@ def test_cone_and_parallel_repr_and_equality():
     par = ts.parallel()
     for u in (ts.parallel(angles=2), ts.parallel(size=5), ts.parallel(shape=3), ts.volume()):
         assert u != par and par != u
+
+
+def test_cone_vec_validation_repr_and_equality():
+    vecs = np.arange(30).reshape((10, 3))
+    kw = dict(src_pos=vecs, det_pos=vecs, det_v=vecs, det_u=vecs)
+    repr(ts.cone_vec(shape=1, **kw))
+    with pytest.raises(TypeError):
+        ts.cone_vec(0, **kw)  # shape is keyword-only
+    with pytest.raises(TypeError):
+        ts.cone_vec(shape=0, **kw)
+    two = np.arange(20).reshape((10, 2))
+    with pytest.raises(TypeError):
+        ts.cone_vec(shape=1, src_pos=two, det_pos=two, det_v=two, det_u=two)
+    with pytest.raises(ValueError):
+        ts.cone_vec(shape=1, src_pos=np.random.normal(size=(10, 3)),
+                    det_pos=np.random.normal(size=(11, 3)),
+                    det_v=np.random.normal(size=(12, 3)), det_u=np.random.normal(size=(13, 3)))
+    x = [[1, 2, 3], [4, 5, 6]]
+    expected = """ts.cone_vec(
+    shape=(10, 10),
+    src_pos=array([[1., 2., 3.],
+       [4., 5., 6.]]),
+    det_pos=array([[1., 2., 3.],
+       [4., 5., 6.]]),
+    det_v=array([[1., 2., 3.],
+       [4., 5., 6.]]),
+    det_u=array([[1., 2., 3.],
+       [4., 5., 6.]]),
+)"""
+    pg = ts.cone_vec(shape=10, src_pos=x, det_pos=x, det_v=x, det_u=x)
+    assert repr(pg) == expected
+    with np.printoptions(legacy="1.13"):
+        assert repr(pg) == expected
+    r = random_cone_vec()
+    assert eval(repr(r), dict(ts=ts, array=np.array)) == r
+    z = np.array([(0, 0, 0)])
+    pg = ts.cone_vec(shape=10, src_pos=z, det_pos=z, det_v=z, det_u=z)
+    for u in (ts.cone_vec(shape=9, src_pos=z, det_pos=z, det_v=z, det_u=z),
+              ts.cone_vec(shape=10, src_pos=z + 1, det_pos=z, det_v=z, det_u=z),
+              ts.cone_vec(shape=10, src_pos=z, det_pos=z + 1, det_v=z, det_u=z),
+              ts.cone_vec(shape=10, src_pos=z, det_pos=z, det_v=z + 1, det_u=z),
+              ts.cone_vec(shape=10, src_pos=z, det_pos=z, det_v=z, det_u=z + 1),
+              ts.cone(angles=2, cone_angle=0.5), ts.volume()):
+        assert pg != u
+    big = ts.cone(angles=10, shape=100, size=np.sqrt(2), cone_angle=0.5).to_vec()
+    assert 10 * big[::10].num_angles == big.num_angles
+    assert np.abs(big[:, ::2].det_v - 2 * big.det_v).sum() == pytest.approx(0.0, abs=1e-7)
+    assert np.abs(big[:, :, ::2].det_pos - big[:, :, 1::2].det_pos).sum() > 1e-7
