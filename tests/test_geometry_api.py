@@ -582,3 +582,49 @@ def test_cone_vec_validation_repr_and_equality():
     assert 10 * big[::10].num_angles == big.num_angles
     assert np.abs(big[:, ::2].det_v - 2 * big.det_v).sum() == pytest.approx(0.0, abs=1e-7)
     assert np.abs(big[:, :, ::2].det_pos - big[:, :, 1::2].det_pos).sum() > 1e-7
+
+
+def test_projection_geometry_interface():
+    """The common interface every projection geometry answers
+    (tomosipo's ``tests/geometry/test_base_projection.py``)."""
+    from tomosipo_gb300.geometry import ProjectionGeometry, is_projection, random_det_vec
+
+    geoms = [ts.cone(size=np.sqrt(2), cone_angle=0.5), ts.cone(size=np.sqrt(2), cone_angle=0.5).to_vec(),
+             ts.cone(angles=10, shape=(5, 3), cone_angle=0.5),
+             ts.cone(size=np.sqrt(2), cone_angle=0.5, angles=11, shape=(10, 10)).to_vec(),
+             random_det_vec(), random_parallel_vec(), random_parallel()]
+    assert not is_projection(ts.volume()) and not is_projection(None)
+    assert ProjectionGeometry().det_shape == (1, 1)
+    with pytest.raises(TypeError):
+        ProjectionGeometry(0)
+    for pg in geoms:
+        assert is_projection(pg) and pg == pg
+        repr(pg)
+        fixed = ts.from_astra(pg.to_astra())
+        assert fixed == ts.from_astra(fixed.to_astra())
+        assert pg.to_vec() == pg.to_vec().to_vec()
+        assert len(pg) == pg.num_angles
+        if pg.is_vec:
+            with pytest.raises(NotImplementedError):
+                pg.angles
+        else:
+            assert len(pg.angles) == pg.num_angles
+        if pg.is_cone:
+            assert pg.src_pos.shape == (pg.num_angles, 3)
+        if pg.is_parallel:
+            assert pg.ray_dir.shape == (pg.num_angles, 3)
+        for name in ("det_pos", "det_v", "det_u"):
+            assert getattr(pg, name).shape == (pg.num_angles, 3)
+        assert vc.cross_product(pg.det_u, pg.det_v) == pytest.approx(pg.det_normal)
+        if pg.is_vec and pg.num_angles > 1:
+            # a detector whose size changes from angle to angle has no single size
+            S = ts.scale(np.abs(np.random.normal(size=(pg.num_angles, 3))) + 0.5)
+            with pytest.raises(ValueError):
+                (S * pg).det_size
+        else:
+            assert len(pg.det_size) == 2
+        assert pg.det_sizes.shape == (pg.num_angles, 2)
+        assert pg.corners.shape == (pg.num_angles, 4, 3)
+        assert pg.reshape(1).det_shape == (1, 1)
+        if pg.is_parallel or pg.is_cone:
+            pg.project_point((0, 0, 0))
