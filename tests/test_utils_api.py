@@ -1,0 +1,91 @@
+"""Interval slicing and vector broadcasting behind geometry indexing
+(tomosipo's ``tests/test_utils.py``, ``tests/test_vector_calc.py``,
+``tests/links/test_numpy.py``), restated. Host only.
+"""
+import numpy as np
+import pytest
+
+import tomosipo_gb300 as ts
+from tomosipo_gb300 import vector_calc as vc
+from tomosipo_gb300.utils import slice_interval
+
+
+class Interval:
+    """A 1-D pixel interval [l, r] of `length` pixels, sliced like an axis."""
+
+    def __init__(self, l, r, length):
+        self.l, self.r, self.length = l, r, length
+
+    def __getitem__(self, key):
+        l, r, length, _ = slice_interval(self.l, self.r, self.length, key)
+        return Interval(l, r, length)
+
+    def __eq__(self, other):
+        return (self.length == other.length and np.all(abs(self.l - other.l) < ts.epsilon)
+                and np.all(abs(self.r - other.r) < ts.epsilon))
+
+    size = property(lambda self: self.r - self.l)
+    pixel_size = property(lambda self: self.size / self.length)
+    center_of_left_pixel = property(lambda self: self.l + self.pixel_size / 2)
+    center = property(lambda self: (self.l + self.r) / 2)
+
+
+def test_slice_interval_basic_cases():
+    assert slice_interval(0, 1, 1, 0) == (0, 1, 1, 1)
+    assert slice_interval(0, 1, 1, slice(None)) == (0, 1, 1, 1)
+    assert slice_interval(0, 0, 1, 0) == (0, 0, 1, 0)
+    assert slice_interval(0, 0, 0, 0) == (0, 0, 0, 1)
+    l0, r0 = np.arange(10), np.arange(10) + 1
+    l1, r1, length1, _ = slice_interval(l0, r0, 10, slice(None))
+    assert np.abs(l0 - l1).sum() == pytest.approx(0) and np.abs(r0 - r1).sum() == pytest.approx(0)
+    assert length1 == 10
+
+
+def test_slice_interval_steps_and_offsets():
+    st = Interval(0, 10, 10)
+    for i in range(1, 5):  # a start offset translates the sliced interval
+        assert st[::5] != st[i::5] and st[::5].length == st[i::5].length
+        assert st[::5].l + i == pytest.approx(st[i::5].l)
+        assert st[::5].r + i == pytest.approx(st[i::5].r)
+        assert st[::5].center + i == pytest.approx(st[i::5].center)
+        assert st[::5].size == st[i::5].size
+    for step in range(1, 10):  # the left-most pixel's centre stays put
+        assert st[::step].center_of_left_pixel == pytest.approx(st.center_of_left_pixel)
+    for length in (0, 5, 6):  # lengths as NumPy slicing counts them
+        st = Interval(0, 1, length)
+        ones = np.ones(length)
+        for start in range(length):
+            for step in (1, 2, 3, 4):
+                assert st[start::step].length == len(ones[start::step])
+                assert st[start::step].pixel_size == pytest.approx(step * st.pixel_size)
+    st = Interval(0, 1, 30)
+    assert st[::2].pixel_size == pytest.approx(2 * st.pixel_size)
+    assert st[1::2].size == pytest.approx(1.0) and st[2::3].size == pytest.approx(1.0)
+    assert st[4::5].size == pytest.approx(1.0)
+    assert st[1::3].center == pytest.approx(st.center)
+    assert st[0::3].center != pytest.approx(st.center)
+    assert st[2::3].center != pytest.approx(st.center)
+
+
+def test_vector_broadcasting():
+    assert vc.broadcast_lengths(1, 1) == 1 and vc.broadcast_lengths(1, 5) == 5
+    assert vc.broadcast_lengths(5, 1) == 5 and vc.broadcast_lengths(3, 3) == 3
+    with pytest.raises(ValueError):
+        vc.broadcast_lengths(2, 3)
+    for a, b in (((3,), (3,)), ((1, 3), (3,)), ((1, 3), (1, 3)), ((3,), (1, 3))):
+        x, y = vc._broadcastv(np.ones(a), np.ones(b))
+        assert x.shape == y.shape == (1, 3)
+    for a, b in (((1, 1, 3), (1, 3)), ((1, 3), (1, 1, 3)), ((2, 3), (3, 3))):
+        with pytest.raises(ValueError):
+            vc._broadcastv(np.ones(a), np.ones(b))
+    A, B = vc._broadcastmm(np.ones((1, 2, 11)), np.ones((1, 11, 3)))
+    assert A.shape == (1, 2, 11) and B.shape == (1, 11, 3)
+    assert vc.matrix_matrix_transform(A, B).shape == (1, 2, 3)
+    with pytest.raises(ValueError):
+        vc._broadcastmm(np.ones((2, 3, 3)), np.ones((3, 3, 3)))
+    assert vc.matrix_transform(np.ones((2, 3, 11)), np.ones((1, 11))).shape == (2, 3)
+
+
+def test_numpy_link_checks_the_shape():
+    with pytest.raises(ValueError):
+        ts.link(ts.volume(shape=10), np.zeros((9, 9, 9), dtype=np.float32))

@@ -45,21 +45,50 @@ def broadcast_lengths(len_a, len_b):
 
 
 def _broadcastv(x, y):
-    n = broadcast_lengths(len(x), len(y))
-    return (np.broadcast_to(x, (n, x.shape[1])), np.broadcast_to(y, (n, y.shape[1])))
+    """Rows of vectors ``(N, k)`` (a single vector ``(k,)`` counts as one row),
+    broadcast to a common number of rows; ``ValueError`` otherwise."""
+    x, y = np.asarray(x), np.asarray(y)
+    s1, s2 = x.shape, y.shape
+    x, y = np.array(x, ndmin=2), np.array(y, ndmin=2)
+    if x.ndim != 2 or y.ndim != 2 or x.shape[1] != y.shape[1]:
+        raise ValueError(f"Arguments of shape {s1} and {s2} could not be broadcast together.")
+    try:
+        n = broadcast_lengths(len(x), len(y))
+    except ValueError:
+        raise ValueError(f"Arguments of shape {s1} and {s2} could not be broadcast together.")
+    return np.broadcast_to(x, (n, x.shape[1])), np.broadcast_to(y, (n, y.shape[1]))
+
+
+def _broadcastmv(m, x):
+    """Matrices ``(N, a, b)`` (or one ``(a, b)``) and vectors ``(N, b)`` (or one
+    ``(b,)``), broadcast to a common N."""
+    m, x = np.asarray(m, dtype=np.float64), np.asarray(x, dtype=np.float64)
+    s1, s2 = m.shape, x.shape
+    m = m[None] if m.ndim == 2 else m
+    x = x[None] if x.ndim == 1 else x
+    if m.ndim != 3 or x.ndim != 2 or m.shape[2] != x.shape[1]:
+        raise ValueError(f"Matrix of shape {s1} cannot transform vectors of shape {s2}.")
+    try:
+        n = broadcast_lengths(len(m), len(x))
+    except ValueError:
+        raise ValueError(f"Matrix of shape {s1} cannot transform vectors of shape {s2}.")
+    return np.broadcast_to(m, (n,) + m.shape[1:]), np.broadcast_to(x, (n, x.shape[1]))
 
 
 def _broadcastmm(m1, m2):
-    m1 = np.array(m1, dtype=np.float64)
-    m2 = np.array(m2, dtype=np.float64)
-    if m1.ndim == 2:
-        m1 = m1[None]
-    if m2.ndim == 2:
-        m2 = m2[None]
-    if m1.shape[1:] != (4, 4) or m2.shape[1:] != (4, 4):
-        raise ValueError("Expected (N, 4, 4) transformation matrices.")
-    n = broadcast_lengths(len(m1), len(m2))
-    return np.broadcast_to(m1, (n, 4, 4)), np.broadcast_to(m2, (n, 4, 4))
+    """Two stacks of matrices ``(N, a, b)`` and ``(N, b, c)`` (single matrices
+    count as one), broadcast to a common N."""
+    m1, m2 = np.asarray(m1, dtype=np.float64), np.asarray(m2, dtype=np.float64)
+    s1, s2 = m1.shape, m2.shape
+    m1 = m1[None] if m1.ndim == 2 else m1
+    m2 = m2[None] if m2.ndim == 2 else m2
+    if m1.ndim != 3 or m2.ndim != 3 or m1.shape[2] != m2.shape[1]:
+        raise ValueError(f"Matrices of shape {s1} and {s2} cannot be multiplied.")
+    try:
+        n = broadcast_lengths(len(m1), len(m2))
+    except ValueError:
+        raise ValueError(f"Matrices of shape {s1} and {s2} could not be broadcast together.")
+    return np.broadcast_to(m1, (n,) + m1.shape[1:]), np.broadcast_to(m2, (n,) + m2.shape[1:])
 
 
 def check_same_shapes(*args):
@@ -110,14 +139,8 @@ def intersect(v_origin, v_direction, plane_origin, plane_normal):
 
 
 def matrix_transform(m, x):
-    """Apply (N, 4, 4) matrices to (N, 4) homogeneous rows (broadcasting N)."""
-    m = np.array(m, dtype=np.float64)
-    x = np.array(x, dtype=np.float64, ndmin=2)
-    if m.ndim == 2:
-        m = m[None]
-    n = broadcast_lengths(len(m), len(x))
-    m = np.broadcast_to(m, (n, 4, 4))
-    x = np.broadcast_to(x, (n, 4))
+    """Apply (N, a, b) matrices to (N, b) rows (broadcasting N): (N, a)."""
+    m, x = _broadcastmv(m, x)
     return np.einsum("nij,nj->ni", m, x)
 
 
