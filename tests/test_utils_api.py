@@ -89,3 +89,20 @@ def test_vector_broadcasting():
 def test_numpy_link_checks_the_shape():
     with pytest.raises(ValueError):
         ts.link(ts.volume(shape=10), np.zeros((9, 9, 9), dtype=np.float32))
+
+
+def test_type_coercion_names_and_errors():
+    from tomosipo_gb300 import types
+
+    assert types.to_tuple(1, 2) == (1, 1) and types.to_tuple((1, 2), n=2) == (1, 2)
+    with pytest.raises(TypeError, match="Expected tuple with 2 elements"):
+        types.to_tuple((1, 2, 3), n=2)
+    assert types.to_shape2d(1) == (1, 1) and types.to_shape2d((5, 3)) == (5, 3)
+    with pytest.raises(TypeError, match="with type <class 'float'>"):
+        types.to_shape2d((5.0, 3))
+    with pytest.raises(TypeError):
+        types.to_shape3d((5, 3))
+    assert types.to_shape_nd(2, 4) == (2, 2, 2, 2)
+    assert types.to_size_nd(1.5, 2) == (1.5, 1.5)
+    with pytest.raises(TypeError):
+        types.to_size2d(-1)

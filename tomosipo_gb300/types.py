@@ -39,7 +39,8 @@ def _to_shape(shape, n):
         if isinstance(s, (np.integer, Integral)) and not isinstance(s, bool):
             out.append(int(s))
         else:
-            raise TypeError(f"Shape must contain only integers. Got {shape}.")
+            raise TypeError(
+                f"Shape must contain only integers. Got {shape} with type {type(s)}.")
     if any(s < 1 for s in out):  # tomosipo/types.py:111-126: a TypeError, as for non-integers
         raise TypeError(f"Shape must be positive. Got {tuple(out)}.")
     return tuple(out)
@@ -60,6 +61,12 @@ def _to_size(size, n):
     if any(s < -EPSILON for s in size):  # tomosipo/types.py:160-170
         raise TypeError(f"Size must be non-negative. Got {size}.")
     return size
+
+
+# The reference's names for the n-dimensional forms (tomosipo/types.py:51-170).
+to_tuple = _as_tuple
+to_shape_nd = _to_shape
+to_size_nd = _to_size
 
 
 def to_size2d(size):
