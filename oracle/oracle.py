@@ -1,11 +1,11 @@
 """ctypes wrapper of the FP64 CPU oracle -- TEST INFRASTRUCTURE ONLY.
 
-Used by tests/ and ``__graft_entry__.smoke()`` as the values the GPU results are
-compared with, and by the CPU-baseline leg of ``bench.py`` as the timed CPU
+Used by tests/ and ``__graft_entry__.smoke()`` as the values the GPU results
+are compared with, and by the CPU-baseline leg of ``bench.py`` as the timed CPU
 baseline; never by the product path. The arithmetic lives in ``oracle.cpp``;
-this file only converts tomosipo
-geometry objects to the C descriptors (volume shape/pos/size and the vector
-rows ``[src_pos or ray_dir, det_pos, det_v, det_u]`` in (z, y, x)).
+this file only converts tomosipo geometry objects to the C descriptors (volume
+shape/pos/size and the vector rows ``[src_pos or ray_dir, det_pos, det_v,
+det_u]`` in (z, y, x)).
 """
 import ctypes
 import os
