@@ -628,3 +628,20 @@ def test_projection_geometry_interface():
         assert pg.reshape(1).det_shape == (1, 1)
         if pg.is_parallel or pg.is_cone:
             pg.project_point((0, 0, 0))
+
+
+def test_operator_needs_a_ray_geometry():
+    """A volume or a detector alone defines no rays: a TypeError at creation
+    (host only; the native projector is made on first use)."""
+    from tomosipo_gb300.geometry import random_det_vec
+
+    vg = ts.volume(shape=8)
+    for pg in (random_det_vec(), ts.volume(shape=8)):
+        with pytest.raises(TypeError, match="parallel or cone"):
+            ts.operator(vg, pg)
+    with pytest.raises(TypeError):
+        ts.operator(ts.parallel(angles=3), vg)  # arguments swapped
+    for pg in (ts.parallel(angles=3), ts.cone(angles=3, cone_angle=0.5)):
+        A = ts.operator(vg, pg)
+        assert A.domain_shape == (8, 8, 8) and A.range_shape == (1, 3, 1)
+        assert A.T.T is A and A.domain == vg and A.range == pg

@@ -24,7 +24,14 @@ def projection_vectors(pg):
     """(kind, rows, cols, vectors[num_angles, 12]) of a projection geometry.
 
     Row layout: [src_pos or ray_dir, det_pos, det_v, det_u], each (z, y, x).
+    Anything but a parallel or cone geometry (vector or not) is a TypeError:
+    a volume, or a detector alone, defines no rays.
     """
+    if not (getattr(pg, "is_parallel", False) or getattr(pg, "is_cone", False)):
+        raise TypeError(
+            "Expected a parallel or cone projection geometry (ts.parallel, ts.parallel_vec, "
+            f"ts.cone, ts.cone_vec). Got {type(pg).__name__}."
+        )
     v = pg.to_vec()
     first = v.src_pos if pg.is_cone else v.ray_dir
     vec = np.concatenate([first, v.det_pos, v.det_v, v.det_u], axis=1)
