@@ -381,6 +381,10 @@ def bench_lpd(torch, ts, device, batch=8, n=128, angles=128, iterations=10, chan
         opt.step()
         return loss
 
+    # cuDNN picks each 3D convolution's algorithm by timing the candidates on
+    # the first call of each shape (the warm-up steps); restored afterwards
+    bench_mode = torch.backends.cudnn.benchmark
+    torch.backends.cudnn.benchmark = True
     for _ in range(warmup):
         step()
     torch.cuda.synchronize()
@@ -392,6 +396,7 @@ def bench_lpd(torch, ts, device, batch=8, n=128, angles=128, iterations=10, chan
     e1.record()
     torch.cuda.synchronize()
     ms = e0.elapsed_time(e1) / steps
+    torch.backends.cudnn.benchmark = bench_mode
     # projector work per step: forward 2 x (FP + BP) per iteration (recomputed),
     # backward one BP and one FP per iteration, each over the batch
     updates = iterations * 3 * 2 * batch * n ** 3 * angles
