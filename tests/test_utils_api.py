@@ -106,3 +106,30 @@ def test_type_coercion_names_and_errors():
     assert types.to_size_nd(1.5, 2) == (1.5, 1.5)
     with pytest.raises(TypeError):
         types.to_size2d(-1)
+
+
+def test_link_coercion_rules():
+    """Links coerce to contiguous fp32 with a UserWarning, reject wrong shapes
+    and unsupported types (tomosipo/links/numpy.py, links/torch.py)."""
+    import warnings
+
+    torch = pytest.importorskip("torch")
+    vg = ts.volume(shape=4)
+    quiet = [np.zeros((4, 4, 4), np.float32), torch.zeros(4, 4, 4)]
+    noisy = [np.zeros((4, 4, 4)), np.zeros((8, 4, 4), np.float32)[::2],
+             torch.zeros(4, 4, 4, dtype=torch.float64), torch.zeros(8, 4, 4)[::2]]
+    for x in quiet:
+        with warnings.catch_warnings():
+            warnings.simplefilter("error")
+            link = ts.link(vg, x)
+        assert link.data.dtype in (np.float32, torch.float32)
+    for x in noisy:
+        with pytest.warns(UserWarning):
+            link = ts.link(vg, x)
+        assert link.data.dtype in (np.float32, torch.float32)
+        assert (link.data.flags["C_CONTIGUOUS"] if isinstance(link.data, np.ndarray)
+                else link.data.is_contiguous())
+    with pytest.raises(ValueError):
+        ts.link(vg, torch.zeros(3, 4, 4))
+    with pytest.raises(ValueError):
+        ts.link(vg, [1, 2, 3])
