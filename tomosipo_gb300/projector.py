@@ -133,7 +133,7 @@ class Projector:
             for h in handles.values():
                 try:
                     _native._lib.tsgb_projector_destroy(h)
-                except Exception:
+                except Exception:  # a finalizer: at interpreter exit CUDA may be torn down
                     pass
 
 

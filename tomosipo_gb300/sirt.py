@@ -148,7 +148,7 @@ class NativeBatch:
     def __del__(self):
         try:
             self.close()
-        except Exception:
+        except Exception:  # a finalizer: at interpreter exit the library may be gone
             pass
 
 
