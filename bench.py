@@ -651,8 +651,11 @@ def main():
     args = p.parse_args()
     global N, ANGLES, DET
     N, ANGLES, DET = WORKLOADS[args.workload]
-    args.steps_ref = max(1, min(args.steps, 2))
-    args.warmup_ref = 0
+    # The reference arm runs the same K timed and W warm-up steps, each one
+    # bounded CPU sample (about 3 s at 512^3), capped so that a large K still
+    # ends in about a minute; its JSON line reports the counts it ran.
+    args.steps_ref = max(1, min(args.steps, 20))
+    args.warmup_ref = max(0, min(args.warmup, 4))
     if args.warmup < 3 and args.impl == "ours":
         print("warning: fewer than 3 warm-up steps", file=sys.stderr)
 

@@ -57,3 +57,26 @@ def test_reference_arm_only_on_rank_zero():
         steps_ref, warmup_ref = 1, 0
 
     assert bench.run_reference(Args(), rank=1, world=2) == 0
+
+
+def test_reference_arm_prints_the_contract_line():
+    """``bench.py --impl reference`` (the oracle on the host cores, small
+    workload here) prints one JSON line with the keys the contract asks for."""
+    import json
+    import subprocess
+    import sys
+
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    out = subprocess.run([sys.executable, "bench.py", "--impl", "reference", "--workload", "c2",
+                          "--steps", "2", "--warmup", "1"], cwd=root, capture_output=True,
+                         text=True, timeout=600)
+    assert out.returncode == 0, out.stderr[-2000:]
+    line = json.loads(out.stdout.strip().splitlines()[-1])
+    assert line["impl"] == "reference" and line["unit"] == "GUPS" and line["value"] > 0
+    assert line["higher_is_better"] is True and "workload" in line["config"]
+    assert line["steps"] == 2 and line["warmup"] == 1  # the counts it ran
+    cb = line["cpu_baseline"]
+    assert cb["kind"] == "port" and cb["cores"] >= 1 and cb["value"] == line["value"] and cb["sample"]
+    e2e = line["e2e"]
+    assert e2e["value"] == line["value"] and e2e["h2d_bytes_per_step"] == 0
+    assert e2e["d2h_bytes_per_step"] == 0
