@@ -5,8 +5,6 @@ The forward projection equals the one-call device path bit for bit; the
 matched backprojection, accumulated chunk by chunk, equals it up to fp32
 summation order. The size threshold is lowered so a small case streams.
 """
-import ctypes
-
 import numpy as np
 import pytest
 

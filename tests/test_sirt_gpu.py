@@ -4,7 +4,7 @@ import pytest
 
 import tomosipo_gb300 as ts
 from oracle import oracle as orc
-from tomosipo_gb300.sirt import BatchedSirt, preconditioners, sirt
+from tomosipo_gb300.sirt import BatchedSirt, sirt
 from tests.helpers import ellipsoid_phantom, rel_l2
 
 torch = pytest.importorskip("torch")

@@ -6,7 +6,6 @@ tile and with odd angle counts (ragged last patch, strip, group and pair).
 """
 import ctypes
 
-import numpy as np
 import pytest
 
 import tomosipo_gb300 as ts

@@ -24,7 +24,6 @@ Steps 1 and 2 are torch element-wise ops and a batched FFT on the device.
 Cone beams whose detector v axis runs along z are supported (circular and
 helical ``cone``/``cone_vec``); other geometries raise ``ValueError``.
 """
-import ctypes
 import math
 
 import numpy as np

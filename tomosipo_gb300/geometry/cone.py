@@ -18,7 +18,7 @@ import numpy as np
 
 from .. import types
 from .base_projection import ProjectionGeometry
-from .cone_vec import ConeVectorGeometry, cone_vec
+from .cone_vec import cone_vec
 from .transform import Transform, EPSILON
 
 

@@ -8,7 +8,6 @@ position ``src_pos``, detector centre ``det_pos`` and pixel vectors ``det_v``,
 import numpy as np
 
 from .. import types
-from .. import vector_calc as vc
 from .base_projection import ProjectionGeometry
 from .det_vec import DetectorVectorGeometry
 from .transform import Transform, EPSILON

@@ -14,7 +14,7 @@ import numpy as np
 
 from .. import types
 from .base_projection import ProjectionGeometry
-from .parallel_vec import ParallelVectorGeometry, parallel_vec
+from .parallel_vec import parallel_vec
 from .transform import Transform, EPSILON
 
 

@@ -10,7 +10,7 @@ import numpy as np
 
 from .. import types
 from .base_projection import ProjectionGeometry
-from .det_vec import DetectorVectorGeometry, det_vec
+from .det_vec import DetectorVectorGeometry
 from .transform import Transform, EPSILON
 
 
