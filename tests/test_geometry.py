@@ -135,6 +135,10 @@ def test_transform_inverse_and_geometry_roundtrip():
 def test_astra_roundtrip(pg):
     # tests/test_astra.py:24-41 (ts.to_astra / ts.from_astra)
     assert ts.from_astra(ts.to_astra(pg)) == pg
+    with pytest.raises(TypeError):
+        ts.from_astra(pg)  # a geometry is not an ASTRA dict
+    with pytest.raises(TypeError):
+        ts.to_astra(ts.to_astra(pg))  # nor is a dict a geometry
 
 
 def test_volume_astra_roundtrip():
