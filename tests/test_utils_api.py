@@ -1,6 +1,8 @@
-"""Interval slicing and vector broadcasting behind geometry indexing
-(tomosipo's ``tests/test_utils.py``, ``tests/test_vector_calc.py``,
-``tests/links/test_numpy.py``), restated. Host only.
+"""Interval slicing and vector broadcasting behind geometry indexing, and the
+argument coercions of the geometry constructors (tomosipo's
+``tests/test_utils.py``, ``tests/test_vector_calc.py``,
+``tests/links/test_numpy.py``, and the examples that ``tests/test_types.py``
+runs from ``tomosipo/types.py``), restated. Host only.
 """
 import numpy as np
 import pytest
@@ -133,3 +135,47 @@ def test_link_coercion_rules():
         ts.link(vg, torch.zeros(3, 4, 4))
     with pytest.raises(ValueError):
         ts.link(vg, [1, 2, 3])
+
+
+_COERCION_ERRORS = [  # the messages tomosipo/types.py documents for each coercion
+    ("to_float_tuple", (("a", 0), 2), "value must contain only floats. Got ('a', 0)."),
+    ("to_size2d", ((3, 2, 1),), "Expected tuple with 2 elements. Got (3, 2, 1)."),
+    ("to_size3d", ((2, 1),), "Expected tuple with 3 elements. Got (2, 1)."),
+    ("to_pos", ((2, 1),), "Expected tuple with 3 elements. Got (2, 1)."),
+    ("to_scalars", (np.ones((1, 3)),),
+     "Value cannot be converted to scalars. Expected shape: (N,). Got shape: (1, 3)."),
+    ("to_scalars", ([],),
+     "Value cannot be converted to scalars. Expected shape: (N,). Got shape: (0,)."),
+    ("to_scalars", ("string",), "Could not convert scalars to np.array. Got: 'string'."),
+    ("to_scalars", (None,), "Could not convert to array of scalars: array contains NaN."),
+    ("to_vec", (np.ones((1, 2)),),
+     "Value cannot be converted to vector. Expected shape: (3,) or (N, 3). Got shape: (1, 2)."),
+    ("to_vec", ("string",), "Could not convert vector to np.array. Got: 'string'."),
+]
+
+
+@pytest.mark.parametrize("name, args, message", _COERCION_ERRORS)
+def test_coercion_error_messages(name, args, message):
+    import re
+
+    from tomosipo_gb300 import types
+
+    with pytest.raises(TypeError, match=re.escape(message)):
+        getattr(types, name)(*args)
+
+
+def test_coercion_values():
+    from tomosipo_gb300 import types
+
+    assert types.to_float_tuple(1, n=2) == (1.0, 1.0)
+    assert types.to_float_tuple((1.0, 2.0), n=2) == (1.0, 2.0)
+    assert types.to_shape3d(1) == (1, 1, 1) and types.to_shape3d((5, 3, 2)) == (5, 3, 2)
+    assert types.to_size2d((5, 3)) == (5.0, 3.0) and types.to_size3d(1) == (1.0, 1.0, 1.0)
+    assert types.to_pos(0) == types.to_pos(0.0) == (0.0, 0.0, 0.0)
+    assert types.to_pos((3, 2, 1)) == (3.0, 2.0, 1.0)
+    assert types.to_scalars(1).shape == (1,)
+    assert np.array_equal(types.to_scalars((1, 1, 1)), np.ones(3))
+    assert types.to_scalars([], accept_empty=True).shape == (0,)
+    assert types.to_vec((1, 1, 1)).shape == (1, 3)
+    assert types.to_vec([(1, 1, 1), (2, 2, 2)]).shape == (2, 3)
+    assert types.to_vec(np.ones((1, 3))).shape == (1, 3)
