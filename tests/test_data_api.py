@@ -58,3 +58,18 @@ def test_project_argument_errors():
         backward(pd)
     with pytest.raises(ValueError):
         fdk(ts.data(ts.volume(shape=4)), ts.data(ts.parallel(angles=2, shape=4)))
+
+
+def test_volume_contiguity_warning_and_projection_idempotency():
+    """tests/test_Data.py:31-34, 75-107: a strided volume is copied with a warning;
+    ``ts.data`` returns the dataset itself for an equal (not identical) geometry and
+    rejects a dataset of another geometry."""
+    vg = ts.volume().reshape(10)
+    with pytest.warns(UserWarning):
+        ts.data(vg, np.ones((20, 10, 10), dtype=np.float32)[::2, ...])
+    pd = ts.data(ts.cone(size=np.sqrt(2), cone_angle=1 / 2, angles=10, shape=20))
+    equal = ts.cone(size=np.sqrt(2), cone_angle=1 / 2, angles=10, shape=20)
+    assert ts.data(equal, pd) is pd
+    for other in (ts.volume(shape=10), ts.cone(size=np.sqrt(2), cone_angle=1 / 2)):
+        with pytest.raises(ValueError):
+            ts.data(other, pd)

@@ -179,3 +179,18 @@ def test_coercion_values():
     assert types.to_vec((1, 1, 1)).shape == (1, 3)
     assert types.to_vec([(1, 1, 1), (2, 2, 2)]).shape == (2, 3)
     assert types.to_vec(np.ones((1, 3))).shape == (1, 3)
+
+
+def test_link_allocates_like_its_data():
+    """tests/test_torch_support.py:32-43: a link's new_zeros / new_full / new_empty
+    give links of the same kind, values and shape (host arrays here)."""
+    torch = pytest.importorskip("torch")
+    vg = ts.volume(shape=8)
+    A = ts.operator(vg, ts.parallel(angles=12, shape=(8, 12)))
+    for vol in (torch.zeros(A.domain_shape), np.zeros(A.domain_shape, dtype=np.float32)):
+        link = ts.link(vg, vol)
+        zeros, full = link.new_zeros(A.domain_shape), link.new_full(A.domain_shape, 1.0)
+        assert type(zeros) is type(link) and type(zeros.data) is type(vol)
+        assert np.allclose(np.asarray(zeros.data), np.asarray(vol))
+        assert np.allclose(np.asarray(full.data), np.asarray(vol) + 1.0)
+        assert link.new_empty(A.domain_shape).shape == link.shape
