@@ -118,3 +118,37 @@ def test_projection_vectors_layout():
     assert np.allclose(vec[:, 3:6], pv.det_pos)
     assert np.allclose(vec[:, 6:9], pv.det_v)
     assert np.allclose(vec[:, 9:12], pv.det_u)
+
+
+# Every other entry point: NULL handles or pointers are rejected with -1 and a
+# message before any CUDA call; destroying NULL is a no-op.
+_NULL_CALLS = {
+    "tsgb_fp_workspace_bytes": (None,),
+    "tsgb_bp_workspace_bytes": (None, 0),
+    "tsgb_projector_shapes": (None, None, None),
+    "tsgb_projector_stats": (None, None, 8),
+    "tsgb_projector_get_tuning": (None, None),
+    "tsgb_projector_set_tuning": (None, None),
+    "tsgb_direct_fp_angles": (None, None, None, 0, 0, 1, 0, None, 0, None),
+    "tsgb_direct_bp_angles": (None, None, None, 0, 0, 1, None, 0, None),
+    "tsgb_copy_sino_angles": (None, None, 1, 1, 1, 0, 1, None),
+    "tsgb_fdk_backproject": (None, None, None, None, 0, None, 0, None),
+    "tsgb_direct_fp_noalloc": (None, None, None, None, 0, None),
+    "tsgb_sirt_batch_create": (None, 0, None),
+    "tsgb_sirt_batch_iterate": (None, 1, None),
+    "tsgb_sirt_batch_iterate_jobs": (None, None, None),
+}
+
+
+@pytest.mark.parametrize("name", sorted(_NULL_CALLS))
+def test_null_arguments_of_every_entry_point(lib, name):
+    assert getattr(lib, name)(*_NULL_CALLS[name]) == -1
+    assert lib.tsgb_last_error().decode()
+    assert lib.tsgb_sirt_batch_destroy(None) == 0
+
+
+def test_null_cases_cover_the_declarations():
+    covered = set(_NULL_CALLS) | {"tsgb_projector_create", "tsgb_direct_fp", "tsgb_direct_bp",
+                                  "tsgb_projector_destroy", "tsgb_sirt_batch_destroy",
+                                  "tsgb_last_error"}
+    assert covered == set(declared_functions())
