@@ -173,7 +173,8 @@ def cpu_baseline_sample(threads=None, angles=None):
         "cores": threads,
         "sample": f"FP + matched BP of {sub.num_angles} of the {ANGLES} angles (every "
         f"{ANGLES // n_angles}th) at full {N}^3 / {DET[0]}x{DET[1]} size; fp64 oracle; "
-        f"FP {t1 - t0:.2f} s, BP {t2 - t1:.2f} s",
+        f"FP {t1 - t0:.2f} s, BP {t2 - t1:.2f} s; a full {ANGLES}-angle FP + BP step "
+        f"extrapolates to {(t2 - t0) * ANGLES / sub.num_angles:.0f} s",
     }
 
 
