@@ -43,6 +43,36 @@ def test_cone_central_ray_chord():
     assert y[7, 0, 7] == pytest.approx(1.0, abs=1e-12)
 
 
+def test_parallel_opposite_angles_see_a_mirrored_detector():
+    # At theta + pi the same rays run backwards and det_u flips (tomosipo's
+    # parallel.to_vec): sinogram column u there is column C - 1 - u at theta.
+    vg = ts.volume(shape=(8, 12, 12), size=(8 / 12, 1, 1))
+    pg = ts.parallel(angles=[0.3, 0.3 + np.pi], shape=(8, 16), size=(8 / 12, 1.4))
+    y = orc.fp(vg, pg, np.random.default_rng(7).random(vg.shape))
+    assert np.abs(y[:, 1, :] - y[:, 0, ::-1]).max() < 1e-12
+
+
+@pytest.mark.parametrize("cone", [False, True])
+def test_rotating_the_volume_is_advancing_the_angle(cone):
+    # Rotating the volume by a quarter turn in the (y, x) plane (np.rot90 over
+    # axes y, x) and projecting at theta equals projecting the original at
+    # theta + pi/2: pins the direction in which angles turn the source and
+    # detector, for both beam types.
+    vg = ts.volume(shape=(8, 12, 12), size=(8 / 12, 1, 1))
+    x = np.random.default_rng(7).random(vg.shape)
+
+    def geometry(theta):
+        if cone:
+            return ts.cone(angles=[theta], shape=(8, 16), size=(8 / 12, 1.4),
+                           src_orig_dist=3, src_det_dist=5)
+        return ts.parallel(angles=[theta], shape=(8, 16), size=(8 / 12, 1.4))
+
+    rotated = np.ascontiguousarray(np.rot90(x, k=1, axes=(1, 2)))
+    a = orc.fp(vg, geometry(0.2), rotated)
+    assert np.abs(a - orc.fp(vg, geometry(0.2 + np.pi / 2), x)).max() < 1e-12
+    assert np.abs(a - orc.fp(vg, geometry(0.2 - np.pi / 2), x)).max() > 1e-2
+
+
 @pytest.mark.parametrize("cone", [False, True])
 def test_oracle_adjoint(cone):
     vg = ts.volume(shape=(12, 14, 16), size=(1, 1.2, 1.1))
