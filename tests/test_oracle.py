@@ -73,6 +73,39 @@ def test_rotating_the_volume_is_advancing_the_angle(cone):
     assert np.abs(a - orc.fp(vg, geometry(0.2 - np.pi / 2), x)).max() > 1e-2
 
 
+@pytest.mark.parametrize("dz, dx", [(0, 3), (2, 0), (1, -2)])
+def test_moving_the_volume_by_whole_voxels_shifts_the_sinogram(dz, dx):
+    # Parallel beam at theta = 0 (det_v along z, det_u along x) with pixel
+    # pitch = voxel pitch: moving the volume by whole voxels shifts the
+    # sinogram by as many pixels (the shadow stays on the detector).
+    x = np.random.default_rng(3).random((6, 10, 10))
+    pg = ts.parallel(angles=[0.0], shape=(12, 20), size=(1.2, 2.0))
+    y = orc.fp(ts.volume(shape=(6, 10, 10), size=(0.6, 1, 1)), pg, x)
+    moved = ts.volume(shape=(6, 10, 10), size=(0.6, 1, 1), pos=(0.1 * dz, 0, 0.1 * dx))
+    expected = np.roll(np.roll(y, dz, axis=0), dx, axis=2)
+    assert np.abs(orc.fp(moved, pg, x) - expected).max() < 1e-12
+
+
+@pytest.mark.parametrize("cone", [False, True])
+def test_scaling_the_whole_geometry_scales_the_integrals(cone):
+    # World units: scaling volume, detector and distances by s scales every
+    # line integral (FP) and every backprojected value (matched BP) by s.
+    s = 2.5
+    x = np.random.default_rng(3).random((6, 10, 10))
+
+    def geometries(f):
+        vg = ts.volume(shape=(6, 10, 10), size=(0.6 * f, f, f))
+        if cone:
+            return vg, ts.cone(angles=5, shape=(12, 20), size=(1.2 * f, 2.0 * f),
+                               src_orig_dist=3 * f, src_det_dist=5 * f)
+        return vg, ts.parallel(angles=5, shape=(12, 20), size=(1.2 * f, 2.0 * f))
+
+    y = orc.fp(*geometries(1), x)
+    assert np.abs(orc.fp(*geometries(s), x) - s * y).max() < 1e-12
+    b = orc.bp_matched(*geometries(1), y)
+    assert np.abs(orc.bp_matched(*geometries(s), y) - s * b).max() < 1e-12
+
+
 @pytest.mark.parametrize("cone", [False, True])
 def test_oracle_adjoint(cone):
     vg = ts.volume(shape=(12, 14, 16), size=(1, 1.2, 1.1))
