@@ -29,7 +29,10 @@
 //
 // Parity pin. No golden FP/BP vectors exist in the reference (its tests are
 // relational, tests/test_Operator.py, tests/test_torch_support.py), so the
-// oracle is pinned by analytic known answers (chord lengths) and by the
+// oracle is pinned by the reference's one numeric FP output (the hollow-box
+// sinogram mean and maximum in notebooks/cupy.ipynb, cell 4), by analytic
+// known answers (chord lengths), by exact identities (adjointness, mirrored
+// opposite angles, quarter-turns, whole-voxel shifts, scaling) and by the
 // reference's own geometry conventions; see tests/test_oracle.py.
 #include <algorithm>
 #include <cmath>
