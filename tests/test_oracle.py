@@ -192,3 +192,22 @@ def test_oracle_matches_golden_fixture(name):
     assert rel_l2(orc.fp(vg, pg, x), data["fp"]) < 1e-12
     assert rel_l2(orc.bp_matched(vg, pg, y), data["bp_matched"]) < 1e-12
     assert rel_l2(orc.bp_bilinear(vg, pg, y), data["bp_bilinear"]) < 1e-12
+
+
+def test_fdk_oracle_reconstructs_a_ball():
+    """The NumPy FDK oracle (oracle/fdk_oracle.py) on the FP64 oracle's
+    projections of a uniform ball (full circular cone scan, 120 angles):
+    FDK's near-exact region recovers the density (measured: interior mean
+    0.9994, worst interior voxel 1.75 % off, outside mean 0.004)."""
+    from oracle import fdk_oracle
+
+    n = 32
+    vg = ts.volume(shape=n, size=1)
+    pg = ts.cone(angles=120, shape=(48, 48), size=1.6, src_orig_dist=3, src_det_dist=4.5)
+    g = (np.arange(n) + 0.5) / n - 0.5
+    Z, Y, X = np.meshgrid(g, g, g, indexing="ij")
+    r2 = Z ** 2 + Y ** 2 + X ** 2
+    rec = fdk_oracle.fdk(vg, pg, orc.fp(vg, pg, (r2 < 0.3 ** 2).astype(np.float64)))
+    inner, outer = r2 < 0.2 ** 2, r2 > 0.4 ** 2
+    assert abs(rec[inner].mean() - 1) < 0.01 and np.abs(rec[inner] - 1).max() < 0.03
+    assert abs(rec[outer].mean()) < 0.02
