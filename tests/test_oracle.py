@@ -1,5 +1,6 @@
-"""The FP64 oracle against known answers, the reference's one numeric output,
-and the committed golden fixtures (CPU only)."""
+"""The FP64 oracle against known answers, exact identities of the
+discretisation, the reference's one numeric output and the committed golden
+fixtures; and the FDK oracle against a known reconstruction (CPU only)."""
 import json
 import os
 
