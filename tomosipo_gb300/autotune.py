@@ -11,8 +11,9 @@ twice the footprint). The best values depend on the volume and detector
 sizes and on the cone angle. ``autotune(A)`` times ``A``'s forward
 projection under candidate settings with CUDA events (coordinate descent from
 the default: element layout, patch rows, group size, patch columns, each from
-the best so far) and sets the fastest on the operator's projector. The batched SIRT solver launches each job's tiles in its
-projector's order, so tuning a job's operator tunes its part of the batch.
+the best so far) and sets the fastest on the operator's projector. The batched
+SIRT solver launches each job's tiles in its projector's order, so tuning a
+job's operator tunes its part of the batch.
 
 Every schedule gives bit-identical results: only the order of independent
 tiles changes. Results are cached per geometry (shapes, beam kind and a hash
@@ -30,6 +31,9 @@ PAIR_LAYOUT = (0, 1)
 PATCH_ROWS = (2, 4, 8, 16, 32)
 GROUP_PAIRS = (8, 16, 32, 64, 128)
 PATCH_COLS = (1, 2, 4, 8, 16)
+# the order in which coordinate descent visits the settings
+SEARCH = (("fp_pair_layout", PAIR_LAYOUT), ("fp_patch_rows", PATCH_ROWS),
+          ("fp_group_pairs", GROUP_PAIRS), ("fp_patch_cols", PATCH_COLS))
 
 _cache = {}
 
@@ -63,6 +67,29 @@ def _time_fp(A, x, y, repeats):
     end.record()
     end.synchronize()
     return start.elapsed_time(end) / repeats
+
+
+def coordinate_descent(start, measure):
+    """Coordinate descent over ``SEARCH`` from the settings ``start``.
+
+    ``measure(tuning) -> ms`` times one candidate. Each setting in turn takes
+    every listed value with the others fixed at the best so far; a candidate is
+    kept only if strictly faster. Returns ``(best, best_ms, start_ms, trials)``.
+    """
+    best = dict(start)
+    best_ms = measure(best)
+    start_ms, trials = best_ms, 1
+    for name, values in SEARCH:
+        measured = best[name]  # this setting's value in the best point so far
+        for v in values:
+            if v == measured:
+                continue
+            cand = dict(best, **{name: v})
+            ms = measure(cand)
+            trials += 1
+            if ms < best_ms:
+                best, best_ms = cand, ms
+    return best, best_ms, start_ms, trials
 
 
 def shape_key(projector):
@@ -99,22 +126,16 @@ def autotune(A, device=None, repeats=None, cache_path=None, verbose=False, key=N
         # about 20 ms of projection per candidate, at least one call
         first = _time_fp(A, x, y, 1)
         reps = repeats or max(1, min(8, int(20.0 / max(first, 1e-3))))
-        best = proj.get_tuning(dev.index)
-        best_ms = _time_fp(A, x, y, reps)
-        default_ms, trials = best_ms, 1
-        for name, values in (("fp_pair_layout", PAIR_LAYOUT), ("fp_patch_rows", PATCH_ROWS),
-                             ("fp_group_pairs", GROUP_PAIRS), ("fp_patch_cols", PATCH_COLS)):
-            for v in values:
-                if v == best[name]:
-                    continue
-                cand = dict(best, **{name: v})
-                proj.set_tuning(dev.index, **cand)
-                ms = _time_fp(A, x, y, reps)
-                trials += 1
-                if verbose:
-                    print(f"autotune {key}: {cand} {ms:.3f} ms")
-                if ms < best_ms:
-                    best, best_ms = cand, ms
+
+        def measure(tuning):
+            proj.set_tuning(dev.index, **tuning)
+            ms = _time_fp(A, x, y, reps)
+            if verbose:
+                print(f"autotune {key}: {tuning} {ms:.3f} ms")
+            return ms
+
+        best, best_ms, default_ms, trials = coordinate_descent(proj.get_tuning(dev.index),
+                                                               measure)
         proj.set_tuning(dev.index, **best)
     result = {"tuning": best, "ms": best_ms, "default_ms": default_ms, "trials": trials}
     _cache[key] = result
