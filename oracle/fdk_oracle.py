@@ -29,17 +29,29 @@ def _frame(vg, pg):
     return S, D, U, V, shape, vs, llc, ref
 
 
-def fdk(vg, pg, y):
-    """FDK reconstruction (fp64 volume) of sinogram ``y`` ((rows, angles, cols))."""
-    S, D, U, V, shape, vs, llc, ref = _frame(vg, pg)
+def _normal_depths(S, D, U, V, ref, t):
+    """Unit detector normal pointing away from the source, SDD and SOD of angle t."""
+    n = np.cross(U[t], V[t])
+    n /= np.linalg.norm(n)
+    if np.dot(D[t] - S[t], n) < 0:
+        n = -n
+    return n, np.dot(D[t] - S[t], n), np.dot(ref - S[t], n)
+
+
+def angle_weights(vg, pg):
+    """dbeta_t / 2: half the source's angular step around the z axis through
+    the reference point (central differences of the unwrapped angle)."""
+    S, _, _, _, _, _, _, ref = _frame(vg, pg)
+    beta = np.unwrap([math.atan2(s[1] - ref[1], s[2] - ref[2]) for s in S])
+    return (np.abs(np.gradient(beta)) if len(S) > 1 else np.array([2 * math.pi])) / 2
+
+
+def filtered(vg, pg, y):
+    """Cosine-weighted, ramp-filtered sinogram (fp64, (rows, angles, cols)): steps
+    1 and 2 of FDK, with the Ram-Lak filter as a direct convolution."""
+    S, D, U, V, _, _, _, ref = _frame(vg, pg)
     y = np.asarray(y, dtype=np.float64)
     R, N, C = y.shape
-    # voxel centres (world)
-    grids = [llc[i] + (np.arange(shape[i]) + 0.5) * vs[i] for i in range(3)]
-    P = np.stack(np.meshgrid(*grids, indexing="ij"), axis=-1).reshape(-1, 3)
-    out = np.zeros(P.shape[0])
-    beta = np.unwrap([math.atan2(s[1] - ref[1], s[2] - ref[2]) for s in S])
-    dbeta = np.abs(np.gradient(beta)) if N > 1 else np.array([2 * math.pi])
     k = np.arange(-(C - 1), C)
     h1 = np.zeros(k.shape)  # unit-pitch Ram-Lak kernel, k = -(C-1) .. C-1
     h1[k == 0] = 0.25
@@ -47,17 +59,29 @@ def fdk(vg, pg, y):
     h1[odd] = -1.0 / (math.pi ** 2 * k[odd].astype(np.float64) ** 2)
     a = np.arange(R) + 0.5 - R / 2
     b = np.arange(C) + 0.5 - C / 2
+    q = np.empty_like(y)
     for t in range(N):
-        n = np.cross(U[t], V[t])
-        n /= np.linalg.norm(n)
-        if np.dot(D[t] - S[t], n) < 0:
-            n = -n
-        sdd = np.dot(D[t] - S[t], n)
-        sod = np.dot(ref - S[t], n)
+        _, sdd, sod = _normal_depths(S, D, U, V, ref, t)
         d = np.linalg.norm(U[t]) * sod / sdd
         X = D[t] + a[:, None, None] * V[t] + b[None, :, None] * U[t]
         p = y[:, t, :] * sdd / np.linalg.norm(X - S[t], axis=-1)
-        q = np.stack([np.convolve(p[r], h1)[C - 1:2 * C - 1] for r in range(R)]) / d
+        q[:, t, :] = np.stack([np.convolve(p[r], h1)[C - 1:2 * C - 1] for r in range(R)]) / d
+    return q
+
+
+def fdk(vg, pg, y):
+    """FDK reconstruction (fp64 volume) of sinogram ``y`` ((rows, angles, cols))."""
+    S, D, U, V, shape, vs, llc, ref = _frame(vg, pg)
+    R, N, C = np.shape(y)
+    # voxel centres (world)
+    grids = [llc[i] + (np.arange(shape[i]) + 0.5) * vs[i] for i in range(3)]
+    P = np.stack(np.meshgrid(*grids, indexing="ij"), axis=-1).reshape(-1, 3)
+    out = np.zeros(P.shape[0])
+    half_dbeta = angle_weights(vg, pg)
+    Q = filtered(vg, pg, y)
+    for t in range(N):
+        n, sdd, sod = _normal_depths(S, D, U, V, ref, t)
+        q = Q[:, t, :]
         # project voxel centres: ray S -> P meets the detector plane at X
         rel = P - S[t]
         depth = rel @ n
@@ -75,5 +99,5 @@ def fdk(vg, pg, y):
                 ii, jj = i0 + di, j0 + dj
                 ok = (ii >= 0) & (ii < R) & (jj >= 0) & (jj < C)
                 val[ok] += (wi * wj)[ok] * q[ii[ok], jj[ok]]
-        out += dbeta[t] / 2 * (sod / depth) ** 2 * val
+        out += half_dbeta[t] * (sod / depth) ** 2 * val
     return out.reshape(tuple(shape))
