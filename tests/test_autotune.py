@@ -93,3 +93,46 @@ def test_cache_file_serves_a_stored_schedule(tmp_path):
 def test_search_values_are_valid_tunings(name, values):
     assert len(set(values)) == len(values) and all(v >= 0 for v in values)
     assert DEFAULT[name] in values
+
+
+def test_full_search_sets_and_caches_the_fastest_schedule(tmp_path, monkeypatch):
+    """``autotune`` end to end with the timing faked and tensors kept on the
+    CPU: it measures every candidate on the operator's projector, leaves the
+    fastest set, returns it and writes it to the cache file."""
+    import contextlib
+    import types
+
+    import torch
+
+    target = dict(DEFAULT, fp_group_pairs=128, fp_patch_cols=1)
+    cost = _separable_cost(target)
+
+    class Operator(_FakeOperator):
+        domain_shape, range_shape = (2, 3, 4), (5, 6, 7)
+
+        def __call__(self, x, out=None):
+            return out
+
+    A = Operator()
+    timed = []
+
+    def fake_time(op, x, y, repeats):
+        assert op is A and x.shape == A.domain_shape and y.shape == A.range_shape
+        timed.append(dict(op.projector.tuning))
+        return cost(op.projector.tuning)
+
+    cpu_torch = types.SimpleNamespace(
+        device=lambda *a: torch.device("cpu"), Generator=torch.Generator, rand=torch.rand,
+        empty=lambda shape, device=None: torch.empty(shape),
+        cuda=types.SimpleNamespace(device=lambda d: contextlib.nullcontext(),
+                                   current_device=lambda: 0))
+    monkeypatch.setattr(at, "torch", cpu_torch)
+    monkeypatch.setattr(at, "_time_fp", fake_time)
+    path = tmp_path / "tuning.json"
+    at._cache.pop("fake-key", None)
+    r = at.autotune(A, cache_path=str(path), key="fake-key")
+    assert not r["cached"] and r["tuning"] == target and A.projector.tuning == target
+    assert r["trials"] == 14 and len(timed) == 15  # the first call sizes the repeats
+    assert r["ms"] == 10.0 and r["default_ms"] == cost(DEFAULT)
+    assert json.loads(path.read_text())["fake-key"]["tuning"] == target
+    at._cache.pop("fake-key", None)
