@@ -1,7 +1,6 @@
 """Host logic of the forward projector's autotuner (``tomosipo_gb300.autotune``):
 the coordinate-descent search on synthetic timings and the cache, with a fake
 operator (no GPU)."""
-import itertools
 import json
 
 import pytest
