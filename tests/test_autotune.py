@@ -135,3 +135,42 @@ def test_full_search_sets_and_caches_the_fastest_schedule(tmp_path, monkeypatch)
     assert r["ms"] == 10.0 and r["default_ms"] == cost(DEFAULT)
     assert json.loads(path.read_text())["fake-key"]["tuning"] == target
     at._cache.pop("fake-key", None)
+
+
+def test_batch_tunes_once_per_job_shape(monkeypatch):
+    """``sirt.autotune_jobs``: one autotuner run per (volume, detector, beam
+    kind), whose schedule every operator of that shape then takes; operators
+    that differ only in their angles share it."""
+    import contextlib
+    import types
+
+    import torch
+
+    from tomosipo_gb300 import sirt
+
+    class Projector(_FakeProjector):
+        def __init__(self, vol, rows, angles, cols, kind):
+            super().__init__()
+            self.vol_shape, self.sino_shape = vol, (rows, angles, cols)
+            self.proj_desc = types.SimpleNamespace(kind=kind)
+
+    ops = []
+    for vol, rows, angles, cols, kind in [((8, 8, 8), 8, 30, 12, 1), ((8, 8, 8), 8, 90, 12, 1),
+                                          ((8, 8, 8), 8, 30, 12, 0), ((16, 16, 16), 16, 30, 24, 1),
+                                          ((8, 8, 8), 8, 60, 12, 1)]:
+        A = _FakeOperator()
+        A.projector = Projector(vol, rows, angles, cols, kind)
+        ops.append(A)
+    runs = []
+
+    def fake_autotune(A, device_index, key):
+        runs.append(key)
+        return {"tuning": dict(DEFAULT, fp_patch_rows=PATCH[len(runs) - 1])}
+
+    PATCH = (2, 4, 16)
+    monkeypatch.setattr(at, "autotune", fake_autotune)
+    monkeypatch.setattr(torch.cuda, "device", lambda d: contextlib.nullcontext())
+    tuning = sirt.autotune_jobs(ops, torch.device("cuda", 0))
+    assert len(runs) == len(set(runs)) == len(tuning) == 3
+    rows = [A.projector.tuning["fp_patch_rows"] for A in ops]
+    assert rows == [2, 2, 4, 16, 2]  # the three cone 8^3 jobs share the first run
