@@ -74,7 +74,9 @@ int tsgb_projector_create(const tsgb_volume_desc* vol,
  * to garbage collection). Synchronises the projector's device. */
 int tsgb_projector_destroy(tsgb_projector* p);
 
-/* Bytes of device workspace ``tsgb_direct_fp`` / ``tsgb_direct_bp`` need. */
+/* Bytes of device workspace ``tsgb_direct_fp`` / ``tsgb_direct_bp`` need
+ * (0 if none); a negative error code for a NULL projector or an unknown
+ * bp_kind. No counterpart in the reference (ASTRA allocates internally). */
 int64_t tsgb_fp_workspace_bytes(const tsgb_projector* p);
 int64_t tsgb_bp_workspace_bytes(const tsgb_projector* p, int32_t bp_kind);
 
