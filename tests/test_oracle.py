@@ -160,6 +160,25 @@ def test_detector_supersampling_is_binned_fine_detector(cone):
         assert rel_l2(orc.fp(vg, pg, x, det_ss=d), binned) < 1e-12
 
 
+@pytest.mark.parametrize("cone", [False, True])
+def test_voxel_supersampling_is_a_summed_fine_volume(cone):
+    """The bilinear BP with d^3 points per voxel == the plain bilinear BP onto
+    a d-times finer volume (each fine voxel weighted by its own volume),
+    summed over d x d x d blocks (exact identity of the discretisation)."""
+    box = dict(size=(0.6, 0.7, 0.8), pos=(0.02, -0.03, 0.01))
+    vg = ts.volume(shape=(6, 7, 8), **box)
+    pg = (
+        ts.cone(angles=5, shape=(9, 11), size=(1.3, 1.7), src_orig_dist=3, src_det_dist=4)
+        if cone
+        else ts.parallel(angles=5, shape=(9, 11), size=(1.3, 1.7))
+    )
+    y = np.random.default_rng(5).random((9, 5, 11))
+    for d in (2, 3):
+        fine = orc.bp_bilinear(ts.volume(shape=(6 * d, 7 * d, 8 * d), **box), pg, y)
+        summed = fine.reshape(6, d, 7, d, 8, d).sum(axis=(1, 3, 5))
+        assert rel_l2(orc.bp_bilinear(vg, pg, y, vox_ss=d), summed) < 1e-12
+
+
 def test_reference_notebook_hollow_box_pin():
     """notebooks/cupy.ipynb cell 4 (reference, ASTRA on GPU): hollow box on a 128^3
     unit cube, ts.parallel(angles=180, shape=128): sinogram mean 0.109146185,
