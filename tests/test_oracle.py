@@ -231,3 +231,15 @@ def test_fdk_oracle_reconstructs_a_ball():
     inner, outer = r2 < 0.2 ** 2, r2 > 0.4 ** 2
     assert abs(rec[inner].mean() - 1) < 0.01 and np.abs(rec[inner] - 1).max() < 0.03
     assert abs(rec[outer].mean()) < 0.02
+
+
+def test_oracle_results_do_not_depend_on_the_thread_count():
+    # The golden fixtures are reproducible on any host only if this holds:
+    # every voxel / pixel is summed by one thread in a fixed order.
+    from tests.golden.make_golden import build_case
+
+    vg, pg, x, y = build_case("cone_vec_helical")
+    for f, arg in ((orc.fp, x), (orc.bp_matched, y), (orc.bp_bilinear, y)):
+        one = f(vg, pg, arg, threads=1)
+        for t in (3, 8):
+            assert np.array_equal(f(vg, pg, arg, threads=t), one), (f.__name__, t)
