@@ -147,10 +147,12 @@ class ClockSampler:
 
 
 # --------------------------------------------------------------------------- CPU baseline
-def cpu_baseline_sample(threads=None, angles=None):
+def cpu_baseline_sample(threads=None, angles=None, keep=False):
     """Time the FP64 oracle (FP + matched BP) on a subset of the workload's angles.
 
-    Returns (GUPS, dict) for the updates processed: 512^3 * n_angles per projection.
+    Returns (GUPS, dict) for the updates processed: 512^3 * n_angles per
+    projection. With ``keep`` the dict also holds the sample's input volume
+    (float32), angle indices and the oracle's FP and BP, for the parity check.
     """
     import tomosipo_gb300 as ts
     from oracle import oracle as orc
@@ -159,23 +161,59 @@ def cpu_baseline_sample(threads=None, angles=None):
     vg, pg = workload_geometry(ts)
     # one angle per thread, at least 8: about 10-20 s of CPU work
     n_angles = angles or max(8, min(threads, 32))
+    idx = np.arange(0, ANGLES, ANGLES // n_angles)[:n_angles]
     sub = pg[:: ANGLES // n_angles][:n_angles]
     rng = np.random.default_rng(2)
-    x = rng.random(vg.shape)
+    x = rng.random(vg.shape, dtype=np.float32)
     t0 = time.perf_counter()
     y = orc.fp(vg, sub, x, threads=threads)
     t1 = time.perf_counter()
-    orc.bp_matched(vg, sub, y, threads=threads)
+    bp = orc.bp_matched(vg, sub, y, threads=threads)
     t2 = time.perf_counter()
     updates = 2 * N ** 3 * sub.num_angles
     gups = updates / (t2 - t0) / 1e9
-    return gups, {
+    info = {
         "cores": threads,
         "sample": f"FP + matched BP of {sub.num_angles} of the {ANGLES} angles (every "
         f"{ANGLES // n_angles}th) at full {N}^3 / {DET[0]}x{DET[1]} size; fp64 oracle; "
         f"FP {t1 - t0:.2f} s, BP {t2 - t1:.2f} s; a full {ANGLES}-angle FP + BP step "
         f"extrapolates to {(t2 - t0) * ANGLES / sub.num_angles:.0f} s",
     }
+    if keep:
+        info["arrays"] = (x, idx, y, bp)
+    return gups, info
+
+
+def _rel_l2(a, b):
+    a = np.asarray(a, dtype=np.float64)
+    b = np.asarray(b, dtype=np.float64)
+    return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300))
+
+
+def parity_vs_oracle(torch, A, device, arrays):
+    """The GPU's full-size operator against the CPU baseline's oracle outputs.
+
+    FP: the sample's angle slices of A(x). BP: A.T of a sinogram holding the
+    oracle's FP (as float32) on the sample's angles and zeros on all others.
+    Adjointness: <A x, y_s> against <x, A.T y_s>, dot products in float64.
+    """
+    x, idx, y_ref, bp_ref = arrays
+    idx_t = torch.as_tensor(idx, device=device)
+    y = A(torch.from_numpy(x).to(device))
+    y_gpu = y.index_select(1, idx_t).cpu().numpy()
+    ys = torch.zeros(A.range_shape, device=device)
+    y_in = y_ref.astype(np.float32)
+    ys[:, idx_t] = torch.from_numpy(y_in).to(device)
+    bp_gpu = A.T(ys).cpu().numpy()
+    lhs = float(np.dot(y_gpu.astype(np.float64).ravel(), y_in.astype(np.float64).ravel()))
+    rhs = float(np.dot(x.astype(np.float64).ravel(), bp_gpu.astype(np.float64).ravel()))
+    adj = abs(lhs - rhs) / (np.linalg.norm(y_gpu.astype(np.float64)) *
+                            np.linalg.norm(y_in.astype(np.float64)))
+    del y, ys
+    torch.cuda.empty_cache()
+    return {"fp_rel_l2": _rel_l2(y_gpu, y_ref), "bp_rel_l2": _rel_l2(bp_gpu, bp_ref),
+            "adjoint": adj, "gate": "rel_l2 <= 1e-5, adjoint <= 1e-6",
+            "angles": f"{len(idx)} of {ANGLES} (every {ANGLES // len(idx)}th), full-size operator"}
 
 
 def run_reference(args, rank, world):
@@ -582,11 +620,12 @@ def run_ours(args, rank, world, local_rank):
     if not args.no_sirt:
         batched = bench_batched_sirt(torch, ts, device, n_jobs=args.sirt_jobs)
         serving = bench_serving(torch, ts, device, n_requests=args.serve_requests)
-    cpu = None
+    cpu = parity = None
     if world == 1 and not args.no_cpu_baseline:
-        gups, info = cpu_baseline_sample()
+        gups, info = cpu_baseline_sample(keep=True)
         cpu = {"value": gups, "unit": "GUPS", "cores": info["cores"], "kind": "port",
                "sample": info["sample"]}
+        parity = parity_vs_oracle(torch, A, device, info.pop("arrays"))
     line = {
         "metric": metric_name(),
         "value": value,
@@ -617,6 +656,7 @@ def run_ours(args, rank, world, local_rank):
             "step_frac": BYTES_PER_UPDATE * value * 1e9 / world / peak / 1e9,
         },
         "cpu_baseline": cpu,
+        "parity": parity,
         "e2e": e2e,
         "batched_sirt": batched,
         "serving": serving,
