@@ -185,17 +185,26 @@ int tsgb_sirt_batch_destroy(tsgb_sirt_batch* b);
  * fp_patch_cols tiles and the angles into groups of fp_group_pairs pairs;
  * a group's tiles over one patch run together, so the volume slab their rays
  * cross is read from HBM once and reused from L2 across the group's angles.
- * Any values >= 1 give bit-identical results. Defaults are set at creation;
- * the Python autotuner times candidates and sets the fastest. Used by
- * tsgb_direct_fp and by the batched SIRT forward pass. No counterpart in the
- * reference (ASTRA's launch shapes are fixed). */
+ * Any values >= 1 give bit-identical results. bp_kernel and bp_shape pick the
+ * matched backprojector and its warp shape; they change only the order of
+ * fp32 sums. Defaults are set at creation; the Python autotuner times
+ * candidates and sets the fastest. Used by tsgb_direct_fp / tsgb_direct_bp and
+ * by the batched SIRT passes. No counterpart in the reference (ASTRA's launch
+ * shapes are fixed). */
 typedef struct {
   int32_t fp_patch_rows;  /* tiles of 32 detector rows per patch (>= 1) */
   int32_t fp_patch_cols;  /* tiles of 8 detector columns per patch (>= 1) */
   int32_t fp_group_pairs; /* pairs of adjacent angles per group (>= 1) */
   int32_t fp_pair_layout; /* 1: volume copies hold neighbour pairs (two 8-byte
                              loads per sample), 0: single voxels (four 4-byte) */
-  int32_t reserved[4];    /* must be 0 */
+  int32_t bp_kernel;      /* matched backprojection of det_v-along-z angles:
+                             1: z-lane warps over a column-major weighted
+                             sinogram, 0: voxel-pair threads over a row-major one */
+  int32_t bp_shape;       /* z-lane warp shape (voxels along the in-plane axis x
+                             voxels along z per lane x warps per block):
+                             0: 4x8x4, 1: 4x8x8, 2: 4x16x8, 3: 4x16x16,
+                             4: 3x16x8, 5: 4x4x4, 6: 4x2x4 */
+  int32_t reserved[2];    /* must be 0 */
 } tsgb_tuning;
 
 int tsgb_projector_get_tuning(const tsgb_projector* p, tsgb_tuning* out);

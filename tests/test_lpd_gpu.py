@@ -65,8 +65,11 @@ def test_checkpoint_equals_stored_activations(dev, exact_convs):
 @pytest.mark.parametrize("activation,rel,abs_", [("relu", 5e-2, 5e-3), ("softplus", 2e-2, 1e-3)])
 def test_gradient_central_differences_16_voxels(dev, exact_convs, activation, rel, abs_):
     """d/d f0_i of sum(w * LPD(g, f0)) by central differences (eps = 1e-3) on 16
-    random voxels, fp32 network. With ReLU a perturbation can cross kinks, so
-    the band is wider; the smooth network is checked tightly."""
+    random voxels, fp32 network. With ReLU a perturbation can cross a kink, where
+    the central difference is no derivative at all: a voxel whose two one-sided
+    differences disagree beyond the band is such a crossing and is left out (at
+    most 3 of 16); the band is also wider. The smooth network is checked tightly
+    on all 16."""
     A, net = _setup(dev, dtype=torch.float32, activation=activation)
     gen = torch.Generator(device="cpu").manual_seed(1)
     g = torch.rand(1, 1, *A.range_shape, generator=gen).to(dev)
@@ -75,8 +78,10 @@ def test_gradient_central_differences_16_voxels(dev, exact_convs, activation, re
     (net(g, f0) * w).sum().backward()
     eps = 1e-3
     idx = torch.randint(0, f0.numel(), (16,), generator=gen).tolist()
-    bad = 0
+    bad = kinks = 0
+    report = []
     with torch.no_grad():
+        l0 = (net(g, f0).double() * w.double()).sum()
         for i in idx:
             e = torch.zeros(f0.numel(), device=dev)
             e[i] = eps
@@ -85,6 +90,11 @@ def test_gradient_central_differences_16_voxels(dev, exact_convs, activation, re
             lm = (net(g, f0 - e).double() * w.double()).sum()
             fd = float((lp - lm) / (2 * eps))
             an = float(f0.grad.view(-1)[i])
-            if abs(fd - an) > rel * abs(an) + abs_:
+            band = rel * abs(an) + abs_
+            report.append((round(an, 5), round(fd, 5)))
+            if activation == "relu" and abs(float((lp - l0) - (l0 - lm)) / eps) > 2 * band:
+                kinks += 1  # one-sided slopes differ: a kink lies within +-eps
+                continue
+            if abs(fd - an) > band:
                 bad += 1
-    assert bad == 0
+    assert bad == 0 and kinks <= 3, (bad, kinks, report)

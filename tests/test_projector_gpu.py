@@ -57,6 +57,8 @@ def _cases():
 
 
 CASES = _cases()
+# matched backprojectors: voxel-pair threads (0) and z-lane warps (1)
+BP_KERNELS = (0, 1)
 
 
 @pytest.fixture(scope="module")
@@ -78,10 +80,12 @@ def test_fp_bp_parity(name, device):
 
     rng = np.random.default_rng(12)
     yy = rng.random(A.range_shape).astype(np.float32)
-    x_gpu = A.T(torch.from_numpy(yy).to(device)).cpu().numpy()
     x_ref = orc.bp_matched(vg, pg, yy)
-    assert rel_l2(x_gpu, x_ref) <= TOL_ORACLE, rel_l2(x_gpu, x_ref)
-    assert adjoint_error(y_gpu, yy, x, x_gpu) <= TOL_ADJOINT
+    for kernel in BP_KERNELS:  # both matched backprojectors
+        A.projector.set_tuning(device.index, bp_kernel=kernel, bp_shape=0)
+        x_gpu = A.T(torch.from_numpy(yy).to(device)).cpu().numpy()
+        assert rel_l2(x_gpu, x_ref) <= TOL_ORACLE, (kernel, rel_l2(x_gpu, x_ref))
+        assert adjoint_error(y_gpu, yy, x, x_gpu) <= TOL_ADJOINT, kernel
 
     B = ts.operator(vg, pg, backprojector="bilinear")
     xb_gpu = B.T(torch.from_numpy(yy).to(device)).cpu().numpy()
@@ -157,9 +161,11 @@ def test_cone_256_subset_parity(device):
     y = A(torch.from_numpy(x).to(device)).cpu().numpy()
     y_ref = orc.fp(vg, pg, x)
     assert rel_l2(y, y_ref) <= TOL_ORACLE, rel_l2(y, y_ref)
-    bp = A.T(torch.from_numpy(y).to(device)).cpu().numpy()
     bp_ref = orc.bp_matched(vg, pg, y)
-    assert rel_l2(bp, bp_ref) <= TOL_ORACLE, rel_l2(bp, bp_ref)
+    for kernel in BP_KERNELS:
+        A.projector.set_tuning(device.index, bp_kernel=kernel, bp_shape=0)
+        bp = A.T(torch.from_numpy(y).to(device)).cpu().numpy()
+        assert rel_l2(bp, bp_ref) <= TOL_ORACLE, (kernel, rel_l2(bp, bp_ref))
 
 
 def _headline_volume(n, seed):
@@ -197,11 +203,16 @@ def test_cone_512_headline_parity(device):
     yy_sub = rng.random((512, 16, 768), dtype=np.float32)
     yy = torch.zeros(A.range_shape, device=device)
     yy[:, ::64] = torch.from_numpy(yy_sub).to(device)
-    bp = A.T(yy).cpu().numpy()
     bp_ref = orc.bp_matched(vg, sub, yy_sub)
-    assert rel_l2(bp, bp_ref) <= TOL_ORACLE, rel_l2(bp, bp_ref)
-    # <A x, yy> = <x, A^T yy>: yy is zero off the 16 angles
-    assert adjoint_error(y_sub, yy_sub, x, bp) <= TOL_ADJOINT
+    # the default matched backprojector at this size (z-lane warps), then the
+    # voxel-pair kernel
+    assert A.projector.get_tuning(device.index)["bp_kernel"] == 1
+    for tuning in (dict(bp_kernel=1, bp_shape=2), dict(bp_kernel=0)):
+        A.projector.set_tuning(device.index, **tuning)
+        bp = A.T(yy).cpu().numpy()
+        assert rel_l2(bp, bp_ref) <= TOL_ORACLE, (tuning, rel_l2(bp, bp_ref))
+        # <A x, yy> = <x, A^T yy>: yy is zero off the 16 angles
+        assert adjoint_error(y_sub, yy_sub, x, bp) <= TOL_ADJOINT, tuning
     del bp_ref
     B = ts.operator(vg, pg, backprojector="bilinear")
     bb = B.T(yy).cpu().numpy()
@@ -300,12 +311,16 @@ def test_matched_bp_edge_geometries(name, device):
     yy = np.random.default_rng(22).random(A.range_shape).astype(np.float32)
     yt = torch.from_numpy(yy).to(device)
     x_ref = orc.bp_matched(vg, pg, yy)
-    xb = A.T(yt)
-    assert rel_l2(xb.cpu().numpy(), x_ref) <= TOL_ORACLE, rel_l2(xb.cpu().numpy(), x_ref)
-    assert adjoint_error(y_gpu, yy, x, xb.cpu().numpy()) <= TOL_ADJOINT
-    acc = xb.clone()
-    ts.operator(vg, pg, additive=True).T(yt, out=acc)
-    assert rel_l2(acc.cpu().numpy(), 2 * x_ref) <= TOL_ORACLE
+    for kernel in BP_KERNELS:
+        A.projector.set_tuning(device.index, bp_kernel=kernel, bp_shape=0)
+        xb = A.T(yt)
+        assert rel_l2(xb.cpu().numpy(), x_ref) <= TOL_ORACLE, (kernel, rel_l2(xb.cpu().numpy(), x_ref))
+        assert adjoint_error(y_gpu, yy, x, xb.cpu().numpy()) <= TOL_ADJOINT, kernel
+        acc = xb.clone()
+        B = ts.operator(vg, pg, additive=True)
+        B.projector.set_tuning(device.index, bp_kernel=kernel, bp_shape=0)
+        B.T(yt, out=acc)
+        assert rel_l2(acc.cpu().numpy(), 2 * x_ref) <= TOL_ORACLE, kernel
 
 
 @pytest.mark.parametrize("d", [2, 3])

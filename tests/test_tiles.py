@@ -81,3 +81,95 @@ def test_weight_pass_writes_each_row_pair_once(rows):
     assert sorted(written) == list(range(-1, rows))
     pad_rows = 2  # rows -2 .. rows + 1 exist in the workspace
     assert min(written) >= -pad_rows and max(written) + 1 <= rows + pad_rows - 1
+
+
+# ---------------------------------------------------------------- z-lane kernels
+# bp_zlane_kernel (tomosipo_gb300/csrc/bp_zlane.cu): a block is kPlanes warps on
+# adjacent planes; blockIdx.x = window * plane_blocks + plane block, blockIdx.y
+# = z range; lane l of a warp owns the kX voxels i0 .. i0 + kX - 1 along a and
+# z = z0 + l + 32 j for j < kRun. Its stores go to the [y][x][z] scratch volume.
+ZLANE_SHAPES = [(4, 8, 4), (4, 8, 8), (4, 16, 8), (4, 16, 16), (3, 16, 8), (4, 4, 4), (4, 2, 4)]
+
+
+def zlane_cover(nx, ny, nz, kx, krun, kplanes, a_is_x):
+    """Write counts per scratch element [y][x][z] of one pass's launch."""
+    n_p, n_a = (ny, nx) if a_is_x else (nx, ny)
+    plane_blocks = -(-n_p // kplanes)
+    windows = -(-n_a // kx)
+    gz = -(-nz // (32 * krun))
+    hits = np.zeros(ny * nx * nz, dtype=np.int32)
+    for bx, by in itertools.product(range(plane_blocks * windows), range(gz)):
+        pb, wb = bx % plane_blocks, bx // plane_blocks
+        for w, lane in itertools.product(range(kplanes), range(32)):
+            ip, i0 = pb * kplanes + w, wb * kx
+            if ip >= n_p:
+                continue  # the warp returns before any access
+            z0 = by * 32 * krun + lane
+            for m in range(kx):
+                ia = i0 + m
+                if ia >= n_a:
+                    break
+                base = (ip * nx + ia) * nz if a_is_x else (ia * nx + ip) * nz
+                for j in range(krun):
+                    z = z0 + 32 * j
+                    if z < nz:
+                        assert 0 <= base + z < hits.size
+                        hits[base + z] += 1
+    return hits
+
+
+@pytest.mark.parametrize("shape", ZLANE_SHAPES)
+@pytest.mark.parametrize("dims", [(9, 13, 70), (4, 4, 1), (33, 5, 257), (1, 1, 1)])
+@pytest.mark.parametrize("a_is_x", [True, False])
+def test_zlane_tiles_cover_every_voxel_once(shape, dims, a_is_x):
+    assert np.all(zlane_cover(*dims, *shape, a_is_x) == 1)
+
+
+@pytest.mark.parametrize("rows, cols", [(1, 1), (7, 40), (32, 32), (62, 65), (512, 768)])
+def test_weight_z_pass_writes_each_padded_pair_once(rows, cols):
+    """bp_weight_z_kernel: blocks of 32 columns x 32 padded pair rows of one
+    angle; every padded pair (theta, iu, r), r < rows + 4, is written once, from
+    shared-memory rows r and r + 1 of its block's 33 (detector rows
+    r0 + k - 2, zero off the detector)."""
+    RP = rows + 4
+    hits = np.zeros((cols, RP), dtype=np.int32)
+    for bx, by in itertools.product(range(-(-cols // 32)), range(-(-RP // 32))):
+        r0 = by * 32
+        for tx, ty in itertools.product(range(32), range(8)):
+            r = r0 + tx
+            if r >= RP:
+                continue
+            for c in range(ty, 32, 8):
+                iu = bx * 32 + c
+                if iu >= cols:
+                    break
+                assert tx + 1 < 33  # shared rows read
+                hits[iu, r] += 1
+    assert np.all(hits == 1)
+
+
+@pytest.mark.parametrize("rows", [1, 2, 5, 64, 511, 512])
+def test_zlane_row_reads_stay_in_the_padded_column(rows):
+    """The fast loop reads anchored rows floor(t) for t in [vmin, vmax + 1) and
+    the clamped loop clamps t to [vmin, vmax]: with vmin = -2 - rows // 2 and
+    vmax = rows - rows // 2, every pair index (2 + rows // 2 + floor(t)) lies
+    in 0 .. rows + 3, the padded column."""
+    ov = rows // 2
+    vmin, vmax = -2 - ov, rows - ov
+    for v0 in range(vmin, vmax + 1):
+        assert 0 <= 2 + ov + v0 <= rows + 3
+
+
+@pytest.mark.parametrize("t", [-300.75, -2.0, -0.5, -1e-6, 0.0, 0.25, 1.0, 255.999, 4e6])
+def test_floor_by_magic_number(t):
+    """The z-lane kernel's exact floor: for |t| < 2^22, t + 1.5 * 2^23 rounded
+    toward -inf is floor(t) + 1.5 * 2^23, and its bits are 0x4B400000 +
+    floor(t). Rounding toward -inf is emulated here with numpy's nextafter."""
+    t32 = np.float32(t)
+    s = np.float32(t32) + np.float32(12582912.0)   # round to nearest
+    exact = float(t32) + 12582912.0
+    if float(s) > exact:                            # step down to round toward -inf
+        s = np.nextafter(s, np.float32(-np.inf))
+    assert float(s) - 12582912.0 == np.floor(float(t32))
+    bits = int(np.array(s, dtype=np.float32).view(np.uint32))
+    assert bits - 0x4B400000 == int(np.floor(float(t32)))

@@ -55,7 +55,8 @@ def test_every_schedule_gives_identical_sinograms(dev, name):
     default = A.projector.get_tuning(dev.index)
     for t in TUNINGS:
         A.projector.set_tuning(dev.index, **t)
-        assert A.projector.get_tuning(dev.index) == t
+        got = A.projector.get_tuning(dev.index)
+        assert {k: got[k] for k in t} == t
         assert torch.equal(A(x), ref), t
         y = torch.ones_like(ref)
         A(x, out=y)
@@ -68,11 +69,11 @@ def test_set_tuning_rejects_bad_values(dev):
     h = A.projector.handle(dev.index)
     lib = _native.load()
     for bad in (dict(fp_patch_rows=0), dict(fp_patch_cols=-1), dict(fp_group_pairs=0),
-                dict(fp_pair_layout=2)):
+                dict(fp_pair_layout=2), dict(bp_kernel=2), dict(bp_shape=-1), dict(bp_shape=7)):
         t = _native.Tuning(**dict(dict(fp_patch_rows=1, fp_patch_cols=1, fp_group_pairs=1), **bad))
         assert lib.tsgb_projector_set_tuning(h, ctypes.byref(t)) == -1
     t = _native.Tuning(fp_patch_rows=1, fp_patch_cols=1, fp_group_pairs=1)
-    t.reserved[2] = 1
+    t.reserved[1] = 1
     assert lib.tsgb_projector_set_tuning(h, ctypes.byref(t)) == -1
     with pytest.raises(ValueError):
         A.projector.set_tuning(dev.index, tile=3)
@@ -93,6 +94,37 @@ def test_autotune_keeps_results_and_caches(dev, tmp_path):
     assert r2["cached"] and B.projector.get_tuning(dev.index) == r["tuning"]
 
 
+BP_TUNINGS = [dict(bp_kernel=0, bp_shape=0)] + [dict(bp_kernel=1, bp_shape=k) for k in range(7)]
+
+
+@pytest.mark.parametrize("name", sorted(_geometries()))
+def test_every_backprojector_shape_agrees(dev, name):
+    """The matched backprojection under every kernel and z-lane warp shape:
+    the same sums in different orders (rel. L2 <= 1e-6 between them), each
+    within the parity tolerance of the FP64 oracle, and additive mode adds."""
+    from oracle import oracle as orc
+    from tests.helpers import TOL_ORACLE, rel_l2
+
+    vg, pg = _geometries()[name]
+    A = ts.operator(vg, pg)
+    B = ts.operator(vg, pg, additive=True)
+    yy = torch.rand(A.range_shape, generator=torch.Generator().manual_seed(4)).to(dev)
+    ref = orc.bp_matched(vg, pg, yy.cpu().numpy())
+    default = A.projector.get_tuning(dev.index)
+    first = None
+    for t in BP_TUNINGS:
+        A.projector.set_tuning(dev.index, **t)
+        B.projector.set_tuning(dev.index, **t)
+        got = A.T(yy)
+        assert rel_l2(got.cpu().numpy(), ref) <= TOL_ORACLE, t
+        first = got if first is None else first
+        assert rel_l2(got.cpu().numpy(), first.cpu().numpy()) <= 1e-6, t
+        acc = got.clone()
+        B.T(yy, out=acc)
+        assert rel_l2(acc.cpu().numpy(), 2 * ref) <= TOL_ORACLE, t
+    A.projector.set_tuning(dev.index, **default)
+
+
 def test_batched_sirt_follows_each_jobs_schedule(dev):
     from tomosipo_gb300.sirt import BatchedSirt, sirt
 
@@ -101,7 +133,8 @@ def test_batched_sirt_follows_each_jobs_schedule(dev):
     for i, t in enumerate(TUNINGS[:3]):
         pg = ts.cone(angles=13 + 2 * i, shape=(37, 45), size=(1.5, 1.8), cone_angle=0.4)
         A = ts.operator(vg, pg)
-        A.projector.set_tuning(dev.index, **t)
+        # jobs on both matched backprojectors (their residual layouts differ)
+        A.projector.set_tuning(dev.index, **t, bp_kernel=i % 2)
         x = torch.rand(A.domain_shape, device=dev)
         jobs.append((A, A(x)))
     b = BatchedSirt(jobs)

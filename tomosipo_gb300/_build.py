@@ -19,7 +19,7 @@ LIBDIR = os.path.join(PKG, "_lib")
 LIBNAME = "libtomosipo_gb300.so"
 LIBPATH = os.path.join(LIBDIR, LIBNAME)
 
-CUDA_SOURCES = ["fp.cu", "bp.cu", "capi.cu", "batch.cu", "noalloc.cu", "supersample.cu"]
+CUDA_SOURCES = ["fp.cu", "bp.cu", "bp_zlane.cu", "capi.cu", "batch.cu", "noalloc.cu", "supersample.cu"]
 CXX_SOURCES = ["plan.cpp"]
 GENCODE = ["-gencode", "arch=compute_103a,code=sm_103a"]
 

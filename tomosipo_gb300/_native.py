@@ -52,7 +52,9 @@ class Tuning(ctypes.Structure):
         ("fp_patch_cols", ctypes.c_int32),
         ("fp_group_pairs", ctypes.c_int32),
         ("fp_pair_layout", ctypes.c_int32),
-        ("reserved", ctypes.c_int32 * 4),
+        ("bp_kernel", ctypes.c_int32),
+        ("bp_shape", ctypes.c_int32),
+        ("reserved", ctypes.c_int32 * 2),
     ]
 
 

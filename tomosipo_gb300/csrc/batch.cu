@@ -144,7 +144,7 @@ int iterate_counts(tsgb_sirt_batch* b, const std::vector<int>& count, cudaStream
       if (it >= count[i]) continue;
       const tsgb_sirt_job& J = b->jobs[i];
       cudaStream_t s = b->streams[i % K];
-      const tsgb::FpSirt sirt{J.sino, J.R, J.residual};
+      const tsgb::FpSirt sirt{J.sino, J.R, J.residual, tsgb::bp_uses_zlane(J.projector) ? 1 : 0};
       e = cudaError_t(tsgb::launch_fp(J.projector, J.vol, nullptr, false, J.fp_workspace, s, &sirt));
       // the forward workspace is free once the residual is written: it holds
       // the first backprojection pass's sum

@@ -19,6 +19,8 @@
 //     profile once per voxel, from one row-pair load. a is x for some angles
 //     and y for others, so the angles run in two passes with different
 //     thread-to-voxel mappings, the second adding onto the first.
+//     (bp_zlane.cu holds the z-lane form of this step, with a column-major
+//     weighted sinogram; the projector's tuning picks one.)
 //  3. bp_general_kernel handles every other angle: it projects the corners of
 //     the voxel's tent footprint onto the detector and tests every pixel in
 //     their bounding box with the forward projector's own ray formula.
@@ -307,13 +309,17 @@ __global__ void __launch_bounds__(128)
     bp_general_kernel(const AngleParams* __restrict__ params,
                       const ColumnEntry* __restrict__ columns, const int* __restrict__ angles,
                       int n_angles, const float2* __restrict__ sinow, float* __restrict__ vol,
-                      DeviceGeometry g, int additive) {
+                      DeviceGeometry g, int additive, int zlayout) {
   const int x = blockIdx.x * 32 + threadIdx.x;
   const int y = blockIdx.y * 4 + threadIdx.y;
   const int z = blockIdx.z;
   if (x >= g.nx || y >= g.ny) return;
   const float xt = float(x - g.ox), yt = float(y - g.oy), zt = float(z - g.oz);
-  const size_t row_stride = (size_t)g.nangles * g.cols;
+  // pair (iv, theta, iu) at base + iv * s_row + iu * s_col: row-major
+  // (rows nangles * cols apart) or column-major (rows adjacent)
+  const size_t RP = size_t(g.rows + 2 * kRowPad);
+  const size_t s_row = zlayout ? 1 : (size_t)g.nangles * g.cols;
+  const size_t s_col = zlayout ? RP : 1;
   float acc = 0.0f;
   for (int n = 0; n < n_angles; ++n) {
     const int theta = __ldg(angles + n);
@@ -345,7 +351,8 @@ __global__ void __launch_bounds__(128)
     const int iu_hi = min(g.cols - 1, (int)ceilf(clamp_coord(umax)) - 1 + g.ou);
     const int iv_lo = max(0, (int)floorf(clamp_coord(vmin)) + 1 + g.ov);
     const int iv_hi = min(g.rows - 1, (int)ceilf(clamp_coord(vmax)) - 1 + g.ov);
-    const float2* base = sinow + ((size_t)kRowPad * g.nangles + theta) * g.cols;
+    const float2* base = zlayout ? sinow + (size_t)theta * g.cols * RP + kRowPad
+                                 : sinow + ((size_t)kRowPad * g.nangles + theta) * g.cols;
     for (int iv = iv_lo; iv <= iv_hi; ++iv) {
       const float vt = float(iv - g.ov);
       for (int iu = iu_lo; iu <= iu_hi; ++iu) {
@@ -354,7 +361,7 @@ __global__ void __launch_bounds__(128)
         const float wa = tent(fmaf(kt, r.ma, r.Xa) - it);
         const float wb = tent(fmaf(kt, r.mb, r.Xb) - jt);
         const float w = wa * wb;
-        if (w > 0.0f) acc = fmaf(w, __ldg(base + (size_t)iv * row_stride + iu).x, acc);
+        if (w > 0.0f) acc = fmaf(w, __ldg(base + iv * s_row + iu * s_col).x, acc);
       }
     }
   }
@@ -690,7 +697,28 @@ int launch_bp_matched(const tsgb_projector* p, float* vol, const float* sino, bo
   cudaStream_t stream = static_cast<cudaStream_t>(stream_);
   const DeviceGeometry& g = p->g;
   if (angle_end < 0) angle_end = g.nangles;
+  // the angles of [angle_begin, angle_end) in each of the three angle lists
+  int off_x, n_ax, off_y, n_ay, off_g, n_g;
+  angle_sub_range(p->host_sep_angles, 0, p->n_sep_ax, angle_begin, angle_end, off_x, n_ax);
+  angle_sub_range(p->host_sep_angles, p->n_sep_ax, p->n_separable_bp, angle_begin, angle_end,
+                  off_y, n_ay);
+  angle_sub_range(p->host_gen_angles, 0, p->n_general_bp, angle_begin, angle_end, off_g, n_g);
   float2* pairs = reinterpret_cast<float2*>(workspace);
+  if (bp_uses_zlane(p)) {
+    // column-major weighted sinogram, z-lane passes into the [y][x][z]
+    // scratch that follows it, then the caller's volume
+    launch_bp_weight_z(p, sino, workspace, angle_begin, angle_end, stream);
+    float* volt = reinterpret_cast<float*>(reinterpret_cast<char*>(workspace) + bp_pairs_bytes(g));
+    const bool written = launch_bp_zlane_separable(p, off_x, n_ax, off_y, n_ay, workspace, volt, vol,
+                                                   additive ? 1 : 0, nullptr, stream);
+    if (n_g > 0 || (!written && !additive)) {
+      const dim3 grid((g.nx + 31) / 32, (g.ny + 3) / 4, g.nz);
+      bp_general_kernel<<<grid, dim3(32, 4), 0, stream>>>(p->d_params, p->d_columns,
+                                                          p->d_gen_angles + off_g, n_g, pairs, vol,
+                                                          g, (additive || written) ? 1 : 0, 1);
+    }
+    return int(cudaGetLastError());
+  }
   const size_t rs = (size_t)g.nangles * g.cols;  // elements between rows
   {
     const dim3 block(32, 8);
@@ -708,12 +736,6 @@ int launch_bp_matched(const tsgb_projector* p, float* vol, const float* sino, bo
   // rows .. rows + kRowPad - 1
   cudaMemsetAsync(pairs, 0, (kRowPad - 1) * rs * sizeof(float2), stream);
   cudaMemsetAsync(pairs + (kRowPad + g.rows) * rs, 0, kRowPad * rs * sizeof(float2), stream);
-  // the angles of [angle_begin, angle_end) in each of the three angle lists
-  int off_x, n_ax, off_y, n_ay, off_g, n_g;
-  angle_sub_range(p->host_sep_angles, 0, p->n_sep_ax, angle_begin, angle_end, off_x, n_ax);
-  angle_sub_range(p->host_sep_angles, p->n_sep_ax, p->n_separable_bp, angle_begin, angle_end,
-                  off_y, n_ay);
-  angle_sub_range(p->host_gen_angles, 0, p->n_general_bp, angle_begin, angle_end, off_g, n_g);
   if (n_ax > 0)
     launch_sep_pass(p, true, p->d_sep_angles + off_x, n_ax, additive ? kBpAdd : kBpSet, pairs,
                     vol, nullptr, nullptr, stream);
@@ -726,7 +748,7 @@ int launch_bp_matched(const tsgb_projector* p, float* vol, const float* sino, bo
     const dim3 grid((g.nx + 31) / 32, (g.ny + 3) / 4, g.nz);
     bp_general_kernel<<<grid, block, 0, stream>>>(p->d_params, p->d_columns,
                                                   p->d_gen_angles + off_g, n_g, pairs, vol, g,
-                                                  (additive || written) ? 1 : 0);
+                                                  (additive || written) ? 1 : 0, 0);
   }
   return int(cudaGetLastError());
 }
@@ -736,6 +758,11 @@ int launch_bp_sirt(const tsgb_projector* p, float* vol, const float* C, const fl
   cudaStream_t stream = static_cast<cudaStream_t>(stream_);
   const float2* pairs = reinterpret_cast<const float2*>(res);
   const int n_ax = p->n_sep_ax, n_ay = p->n_separable_bp - p->n_sep_ax;
+  if (bp_uses_zlane(p)) {
+    // the residual is column-major; scratch holds the [y][x][z] sum
+    launch_bp_zlane_separable(p, 0, n_ax, n_ax, n_ay, res, scratch, vol, 2, C, stream);
+    return int(cudaGetLastError());
+  }
   const int* ax = p->d_sep_angles;
   const int* ay = p->d_sep_angles + n_ax;
   if (n_ax > 0 && n_ay > 0) {

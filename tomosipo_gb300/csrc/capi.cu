@@ -172,8 +172,10 @@ int64_t tsgb_bp_workspace_bytes(const tsgb_projector* p, int32_t bp_kind) {
                              : 0;
   if (bp_kind != TSGB_BP_MATCHED) return fail(TSGB_ERR_INVALID, "unknown bp_kind");
   if (p->fine) return fine_sino_bytes(p) + tsgb_bp_workspace_bytes(p->fine, bp_kind);
-  // row-pair weighted sinogram: two floats per pixel, kRowPad padding rows
-  return int64_t(p->g.rows + 2 * tsgb::kRowPad) * p->g.nangles * p->g.cols * int64_t(2 * sizeof(float));
+  // row-pair weighted sinogram (two floats per pixel, kRowPad padding rows),
+  // then the z-lane kernel's [y][x][z] scratch volume (either kernel may run)
+  return tsgb::bp_pairs_bytes(p->g) +
+         (p->n_separable_bp > 0 ? tsgb::bp_volume_bytes(p->g) : int64_t(0));
 }
 
 int tsgb_projector_shapes(const tsgb_projector* p, int64_t vol_shape[3], int64_t sino_shape[3]) {
@@ -336,8 +338,11 @@ int tsgb_projector_stats(const tsgb_projector* p, int64_t* out, int32_t n) {
   const int64_t chunk = tsgb::fp_angle_chunk(f->g);
   const int64_t fp_launches =
       int64_t(f->layouts.size()) + (f->g.nangles + chunk - 1) / chunk + extra;
+  // weight pass, one launch per separable pass, the z-lane kernel's transpose
+  // out of its scratch, the general kernel
   const int64_t bp_launches = chunks + (f->n_sep_ax > 0 ? 1 : 0) +
                               (f->n_separable_bp - f->n_sep_ax > 0 ? 1 : 0) +
+                              (tsgb::bp_uses_zlane(f) && f->n_separable_bp > 0 ? 1 : 0) +
                               ((f->n_general_bp > 0 || f->n_separable_bp == 0) ? 1 : 0) + extra;
   const int64_t vals[8] = {int64_t(f->layouts.size()),
                            f->n_separable_bp,
@@ -366,9 +371,12 @@ int tsgb_projector_set_tuning(tsgb_projector* p, const tsgb_tuning* t) {
     return fail(TSGB_ERR_INVALID, "tuning values must be >= 1");
   if (t->fp_pair_layout != 0 && t->fp_pair_layout != 1)
     return fail(TSGB_ERR_INVALID, "fp_pair_layout must be 0 or 1");
-  for (int i = 0; i < 4; ++i)
+  if (t->bp_kernel != 0 && t->bp_kernel != 1) return fail(TSGB_ERR_INVALID, "bp_kernel must be 0 or 1");
+  if (t->bp_shape < 0 || t->bp_shape > 6) return fail(TSGB_ERR_INVALID, "bp_shape must lie in 0 .. 6");
+  for (int i = 0; i < 2; ++i)
     if (t->reserved[i] != 0) return fail(TSGB_ERR_INVALID, "reserved tuning fields must be 0");
-  (p->fine ? p->fine : p)->tuning = *t;  // the projector that runs the FP
+  // the projector that runs the FP and the matched BP
+  (p->fine ? p->fine : p)->tuning = *t;
   return TSGB_OK;
 }
 

@@ -305,10 +305,21 @@ __device__ __forceinline__ void fp_ray_pair(const AngleParams& apa, const AngleP
 // pair and the second of the pair one row up. The plain recipe computes the
 // same products with separate operations (y - A(x), times R, then the
 // backprojector's W pass), rounded the same way.
+// With s.zlayout the pairs are column-major (bp_weight_z_kernel): pixel
+// (iv, theta, iu) is the first value of pair (theta, iu, iv + kRowPad) and the
+// second of the pair before it.
 __device__ __forceinline__ void sirt_residual(const FpSirt& s, const DeviceGeometry& g,
                                               long long idx, float total, float W) {
   const float r = __fmul_rn(__fsub_rn(__ldg(s.y + idx), total), __ldg(s.R + idx));
   const float v = __fmul_rn(W, r);
+  if (s.zlayout) {
+    const long long iu = idx % g.cols, rest = idx / g.cols;
+    const long long theta = rest % g.nangles, iv = rest / g.nangles;
+    float* e = s.res + 2 * ((theta * g.cols + iu) * (g.rows + 2 * kRowPad) + iv + kRowPad);
+    e[0] = v;
+    e[-1] = v;
+    return;
+  }
   const long long rs = (long long)g.nangles * g.cols;
   float* e = s.res + 2 * (idx + kRowPad * rs);
   e[0] = v;
@@ -463,6 +474,13 @@ tsgb_tuning default_tuning(const tsgb_projector* p) {
   t.fp_patch_rows = 256 / kFpRows;
   t.fp_patch_cols = 32 / kFpCols;
   t.fp_group_pairs = 32;
+  // Matched backprojection: z-lane warps of 4 voxels x 16 z per lane x 8
+  // planes for volumes of 448 or more voxels along z (512^3 / 1024 angles:
+  // 124.8 ms against 144.5 ms for the voxel-pair kernel); below that a warp's
+  // 512 z would leave lanes idle, and the voxel-pair kernel is faster at 256^3
+  // (6.76 ms against 7.2 ms for the best z-lane shape).
+  t.bp_kernel = p->g.nz >= 448 ? 1 : 0;
+  t.bp_shape = 2;
   return t;
 }
 

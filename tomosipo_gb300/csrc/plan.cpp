@@ -50,6 +50,74 @@ bool finite3(const V3& v) {
 
 }  // namespace
 
+std::string reduce_angle(const double* row, bool cone, const double vs[3], const double origin[3],
+                         int rows, int cols, int ov, int ou, bool allow_separable, int t,
+                         AngleFrame* f) {
+  V3 src_w{{row[0], row[1], row[2]}}, det_w{{row[3], row[4], row[5]}};
+  V3 v_w{{row[6], row[7], row[8]}}, u_w{{row[9], row[10], row[11]}};
+  if (!finite3(src_w) || !finite3(det_w) || !finite3(v_w) || !finite3(u_w))
+    return "non-finite geometry vector at angle " + std::to_string(t);
+  if (norm(u_w) == 0.0 || norm(v_w) == 0.0 || norm(cross(u_w, v_w)) == 0.0)
+    return "degenerate detector pixel vectors at angle " + std::to_string(t);
+  // Anchored pixel origin: centre of pixel (ov, ou) (world units).
+  const V3 dc_w = axpy(axpy(det_w, ov + 0.5 - 0.5 * rows, v_w), ou + 0.5 - 0.5 * cols, u_w);
+  V3 ref;  // central ray direction in voxel units
+  for (int i = 0; i < 3; ++i) {
+    f->U[i] = u_w[i] / vs[i];
+    f->V[i] = v_w[i] / vs[i];
+    f->Dc[i] = (dc_w[i] - origin[i]) / vs[i];
+    f->S[i] = (src_w[i] - origin[i]) / vs[i];  // source (cone)
+    f->R[i] = src_w[i] / vs[i];                // ray direction (parallel)
+    ref[i] = cone ? (det_w[i] - src_w[i]) / vs[i] : f->R[i];
+  }
+  if (norm(ref) == 0.0) return "zero ray direction at angle " + std::to_string(t);
+  const int d = argmax_abs(ref, -1);
+  const V3 Vv{{f->V[0], f->V[1], f->V[2]}};
+  const int b = argmax_abs(Vv, d);
+  const int a = 3 - d - b;
+  f->d = d;
+  f->a = a;
+  f->b = b;
+  const double vn = norm(Vv);
+  f->separable = allow_separable && std::fabs(f->V[d]) <= 1e-12 * vn &&
+                 std::fabs(f->V[a]) <= 1e-12 * vn;
+  if (f->separable) {
+    f->V[d] = 0.0;
+    f->V[a] = 0.0;
+  }
+  // Ray coefficients over (1, ut, vt).
+  if (cone) {
+    const double D[3] = {f->Dc[0] - f->S[0], f->Dc[1] - f->S[1], f->Dc[2] - f->S[2]};
+    if (D[d] == 0.0) return "detector centre lies in the source's dominant plane";
+    const double sc = 1.0 / D[d];  // normalise so den = 1 at the anchored pixel
+    const double ed[3] = {D[d], f->U[d], f->V[d]};
+    const double ea[3] = {D[a], f->U[a], f->V[a]};
+    const double eb[3] = {D[b], f->U[b], f->V[b]};
+    for (int j = 0; j < 3; ++j) {
+      f->e[j] = ed[j] * sc;
+      f->ca[j] = (f->S[a] * ed[j] - f->S[d] * ea[j]) * sc;
+      f->ma[j] = ea[j] * sc;
+      f->cb[j] = (f->S[b] * ed[j] - f->S[d] * eb[j]) * sc;
+      f->mb[j] = eb[j] * sc;
+    }
+  } else {
+    if (f->R[d] == 0.0) return "ray parallel to every volume plane";
+    const double sa = f->R[a] / f->R[d], sb = f->R[b] / f->R[d];
+    f->e[0] = 1.0;
+    f->e[1] = f->e[2] = 0.0;
+    f->ca[0] = f->Dc[a] - f->Dc[d] * sa;
+    f->ca[1] = f->U[a] - f->U[d] * sa;
+    f->ca[2] = f->V[a] - f->V[d] * sa;
+    f->cb[0] = f->Dc[b] - f->Dc[d] * sb;
+    f->cb[1] = f->U[b] - f->U[d] * sb;
+    f->cb[2] = f->V[b] - f->V[d] * sb;
+    f->ma[0] = sa;
+    f->mb[0] = sb;
+    f->ma[1] = f->ma[2] = f->mb[1] = f->mb[2] = 0.0;
+  }
+  return std::string();
+}
+
 std::string build_plan(const tsgb_volume_desc* vol, const tsgb_projection_desc* proj,
                        int voxel_ss, int det_ss, tsgb_projector* p,
                        std::vector<ColumnEntry>* columns, std::vector<int>* sep_angles,
@@ -109,80 +177,26 @@ std::string build_plan(const tsgb_volume_desc* vol, const tsgb_projection_desc* 
   bil_fast->clear();
   bil_slow->clear();
 
+  const double vs_a[3] = {vs[0], vs[1], vs[2]}, origin_a[3] = {origin[0], origin[1], origin[2]};
   for (int t = 0; t < g.nangles; ++t) {
     const double* row = proj->vectors + 12 * size_t(t);
-    V3 src_w{{row[0], row[1], row[2]}}, det_w{{row[3], row[4], row[5]}};
-    V3 v_w{{row[6], row[7], row[8]}}, u_w{{row[9], row[10], row[11]}};
-    if (!finite3(src_w) || !finite3(det_w) || !finite3(v_w) || !finite3(u_w))
-      return "non-finite geometry vector at angle " + std::to_string(t);
-    if (norm(u_w) == 0.0 || norm(v_w) == 0.0 || norm(cross(u_w, v_w)) == 0.0)
-      return "degenerate detector pixel vectors at angle " + std::to_string(t);
-
-    // Anchored pixel origin: centre of pixel (ov, ou) (world units).
-    V3 dc_w = axpy(axpy(det_w, g.ov + 0.5 - 0.5 * g.rows, v_w), g.ou + 0.5 - 0.5 * g.cols, u_w);
-    // To anchored voxel coordinates.
-    V3 U, V, Dc, S, R;
-    for (int i = 0; i < 3; ++i) {
-      U[i] = u_w[i] / vs[i];
-      V[i] = v_w[i] / vs[i];
-      Dc[i] = (dc_w[i] - origin[i]) / vs[i];
-      S[i] = (src_w[i] - origin[i]) / vs[i];  // source (cone)
-      R[i] = src_w[i] / vs[i];                // ray direction (parallel)
-    }
-    V3 ref;  // central ray direction in voxel units
-    if (cone) {
-      for (int i = 0; i < 3; ++i) ref[i] = (det_w[i] - src_w[i]) / vs[i];
-    } else {
-      ref = R;
-    }
-    if (norm(ref) == 0.0) return "zero ray direction at angle " + std::to_string(t);
-
+    AngleFrame f;
+    const std::string err =
+        reduce_angle(row, cone, vs_a, origin_a, g.rows, g.cols, g.ov, g.ou, det_ss == 1, t, &f);
+    if (!err.empty()) return err;
+    const V3 u_w{{row[9], row[10], row[11]}}, v_w{{row[6], row[7], row[8]}};
+    const V3 src_w{{row[0], row[1], row[2]}};
+    const V3 U{{f.U[0], f.U[1], f.U[2]}}, V{{f.V[0], f.V[1], f.V[2]}};
+    const V3 Dc{{f.Dc[0], f.Dc[1], f.Dc[2]}}, S{{f.S[0], f.S[1], f.S[2]}};
+    const V3 R{{f.R[0], f.R[1], f.R[2]}};
     AngleParams& ap = p->host_params[t];
-    const int d = argmax_abs(ref, -1);
-    const int b = argmax_abs(V, d);
-    const int a = 3 - d - b;
+    const int d = f.d, a = f.a, b = f.b;
     ap.d = d;
     ap.a = a;
     ap.b = b;
-    const double vn = norm(V);
-    const bool separable = det_ss == 1 && std::fabs(V[d]) <= 1e-12 * vn && std::fabs(V[a]) <= 1e-12 * vn;
-    if (separable) {
-      V[d] = 0.0;
-      V[a] = 0.0;
-    }
+    const bool separable = f.separable;
     ap.separable = separable ? 1 : 0;
-
-    // Ray coefficients over (1, ut, vt).
-    double e[3], ca[3], ma[3], cb[3], mb[3];
-    if (cone) {
-      V3 D = sub(Dc, S);
-      if (D[d] == 0.0) return "detector centre lies in the source's dominant plane";
-      const double sc = 1.0 / D[d];  // normalise so den = 1 at the anchored pixel
-      const double ed[3] = {D[d], U[d], V[d]};
-      const double ea[3] = {D[a], U[a], V[a]};
-      const double eb[3] = {D[b], U[b], V[b]};
-      for (int j = 0; j < 3; ++j) {
-        e[j] = ed[j] * sc;
-        ca[j] = (S[a] * ed[j] - S[d] * ea[j]) * sc;
-        ma[j] = ea[j] * sc;
-        cb[j] = (S[b] * ed[j] - S[d] * eb[j]) * sc;
-        mb[j] = eb[j] * sc;
-      }
-    } else {
-      if (R[d] == 0.0) return "ray parallel to every volume plane";
-      const double sa = R[a] / R[d], sb = R[b] / R[d];
-      e[0] = 1.0;
-      e[1] = e[2] = 0.0;
-      ca[0] = Dc[a] - Dc[d] * sa;
-      ca[1] = U[a] - U[d] * sa;
-      ca[2] = V[a] - V[d] * sa;
-      cb[0] = Dc[b] - Dc[d] * sb;
-      cb[1] = U[b] - U[d] * sb;
-      cb[2] = V[b] - V[d] * sb;
-      ma[0] = sa;
-      mb[0] = sb;
-      ma[1] = ma[2] = mb[1] = mb[2] = 0.0;
-    }
+    const double *e = f.e, *ca = f.ca, *ma = f.ma, *cb = f.cb, *mb = f.mb;
     for (int j = 0; j < 3; ++j) {
       ap.e[j] = float(e[j]);
       ap.ca[j] = float(ca[j]);

@@ -133,6 +133,25 @@ struct tsgb_projector {
 
 namespace tsgb {
 
+// One angle's detector frame and ray coefficients in anchored voxel
+// coordinates (fp64), shared by build_plan and the no-allocation path.
+struct AngleFrame {
+  double U[3], V[3];   // det_u, det_v per voxel
+  double Dc[3];        // centre of the anchored pixel (ov, ou)
+  double S[3], R[3];   // source position (cone) / ray direction (parallel)
+  int d, a, b;         // dominant axis, in-plane axes (b: the one det_v runs along)
+  bool separable;      // det_v has no d or a component (then snapped to exact zeros)
+  double e[3], ca[3], ma[3], cb[3], mb[3];  // ray coefficients over (1, ut, vt)
+};
+
+// Reduce row t of a projection's vectors ([src|ray, det_pos, det_v, det_u]);
+// vs / origin: voxel size and the anchor voxel's centre (world). Returns "" or
+// the error message (non-finite vectors, zero or parallel det_u / det_v, a
+// zero ray direction, a degenerate cone frame).
+std::string reduce_angle(const double* row, bool cone, const double vs[3], const double origin[3],
+                         int rows, int cols, int ov, int ou, bool allow_separable, int t,
+                         AngleFrame* f);
+
 // Host-side construction of the per-angle tables in fp64 (plan.cpp). Fills
 // p->g, p->host_params, p->layouts and the column table; returns an empty
 // string on success, else the error message.
@@ -165,12 +184,40 @@ void set_last_error(const std::string& msg);
 // SIRT epilogue of the forward projection: instead of a sinogram it writes
 // res = W * (R * (y - A x)) in the backprojector's row-pair layout, where W is
 // each ray's plane step (see bp_weight_kernel). res holds
-// 2 * (rows + 2 kRowPad) * nangles * cols floats whose padding rows are zero.
+// 2 * (rows + 2 kRowPad) * nangles * cols floats whose padding rows are zero;
+// zlayout: column-major pairs (bp_weight_z_kernel), else row-major.
 struct FpSirt {
   const float* y;  // measured sinogram
   const float* R;  // per-ray weights (sinogram-shaped)
   float* res;
+  int zlayout;
 };
+
+// The matched backprojector of det_v-along-z angles is the z-lane kernel
+// (bp_zlane.cu, column-major weighted sinogram) unless the tuning picks the
+// voxel-pair kernel (bp.cu, row-major) or the volume's (y, x) plane is too
+// large for the z-lane grid (fewer than 2^32 voxel columns keep it below 2^31
+// blocks for every shape, which hold at least 8 columns per block).
+inline bool bp_uses_zlane(const tsgb_projector* p) {
+  return p->tuning.bp_kernel == 1 && int64_t(p->g.nx) * p->g.ny < (int64_t(1) << 32);
+}
+inline int zlane_shape(const tsgb_projector* p) { return p->tuning.bp_shape; }
+
+// Bytes of the matched backprojection's weighted sinogram (either layout),
+// rounded up to 256; the z-lane kernel's [y][x][z] scratch volume follows it.
+int64_t bp_pairs_bytes(const DeviceGeometry& g);
+int64_t bp_volume_bytes(const DeviceGeometry& g);
+
+// Column-major row-pair weighted sinogram (float pairs) of angles
+// angle_begin .. angle_end - 1 (bp_zlane.cu).
+int launch_bp_weight_z(const tsgb_projector* p, const float* sino, float* sinoz, int angle_begin,
+                       int angle_end, void* stream);
+// Both z-lane passes over the separable angle lists (offsets into
+// p->d_sep_angles) into the [y][x][z] scratch volt, then vol (=, +=, SIRT)
+// from it (out_mode 0 / 1 / 2; C for SIRT). False if there are no such angles.
+bool launch_bp_zlane_separable(const tsgb_projector* p, int off_x, int n_ax, int off_y, int n_ay,
+                               const float* sinoz, float* volt, float* vol, int out_mode,
+                               const float* C, void* stream);
 
 // Kernel launchers (fp.cu, bp.cu). All return cudaGetLastError() as int.
 // With `sirt` the forward projection writes the SIRT residual instead of sino.
