@@ -30,12 +30,22 @@
 // loaded (on the first use of this entry point under CUDA's default lazy module
 // loading, at library load with CUDA_MODULE_LOADING=EAGER) until the process exits.
 //
+// The per-angle parameters reach the device as kernel arguments (chunks of
+// kParamChunk angles, written into the static parameter array by a small copy
+// kernel on the caller's stream), so a call issues no host-to-device memcpy and
+// keeps no host buffer that a later call could overwrite before it is read.
+//
 // The arithmetic is the forward projector of fp.cu (Joseph's method on the
 // dominant axis of each angle, bilinear in-plane, scaled by the plane step), with
-// every ray's coefficients computed from the per-angle parameters.
+// every ray's coefficients computed from the per-angle parameters. The per-angle
+// reduction (frame, dominant axis, ray coefficients, and the checks that reject
+// degenerate detectors) is plan.cpp's reduce_angle, the same function the
+// regular projector's planner uses.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cmath>
+#include <cstring>
 #include <mutex>
 #include <string>
 
@@ -49,6 +59,7 @@ constexpr int kMaxDevices = 64;
 constexpr int kRows = 32;  // threads along detector rows (one warp)
 constexpr int kCols = 8;   // warps along detector columns
 constexpr float kMaxSlope = 64.0f;
+constexpr int kParamChunk = 64;  // angles per parameter-copy launch (16 KiB of arguments)
 
 static __device__ __align__(256) float g_scratch[kScratchFloats];
 static __device__ __align__(256) tsgb::AngleParams g_params[kMaxAngles];
@@ -57,6 +68,21 @@ std::mutex g_mutex;                           // guards the host staging buffer 
 tsgb::AngleParams g_host_params[kMaxAngles];  // host staging of the per-angle parameters
 void* g_scratch_ptr[kMaxDevices] = {};  // device addresses, resolved once per device
 void* g_params_ptr[kMaxDevices] = {};
+
+// One chunk of per-angle parameters, passed by value as a kernel argument.
+struct ParamChunk {
+  tsgb::AngleParams p[kParamChunk];
+};
+
+// Copies `count` parameter entries from the launch's arguments to dst.
+__global__ void noalloc_params_kernel(const __grid_constant__ ParamChunk chunk, int count,
+                                      tsgb::AngleParams* __restrict__ dst) {
+  static_assert(sizeof(tsgb::AngleParams) % sizeof(int4) == 0, "16-byte words");
+  const int4* src = reinterpret_cast<const int4*>(chunk.p);
+  int4* out = reinterpret_cast<int4*>(dst);
+  const int words = count * int(sizeof(tsgb::AngleParams) / sizeof(int4));
+  for (int i = threadIdx.x; i < words; i += blockDim.x) out[i] = src[i];
+}
 
 int fail(int code, const std::string& msg) {
   tsgb::set_last_error(msg);  // read back through tsgb_last_error()
@@ -131,13 +157,6 @@ __global__ void __launch_bounds__(kRows* kCols)
     *out = total;
 }
 
-int argmax_abs3(const double* v, int skip) {
-  int best = -1;
-  for (int i = 0; i < 3; ++i)
-    if (i != skip && (best < 0 || std::fabs(v[i]) > std::fabs(v[best]))) best = i;
-  return best;
-}
-
 // Per-angle parameters (fp64 -> fp32) of the forward projector, written into
 // g_host_params; returns "" or an error message. Layout offsets go to lay_*.
 std::string plan_angles(const tsgb_volume_desc* vol, const tsgb_projection_desc* proj,
@@ -155,60 +174,21 @@ std::string plan_angles(const tsgb_volume_desc* vol, const tsgb_projection_desc*
   *n_layouts = 0;
   long long used = 0;
   for (int t = 0; t < g->nangles; ++t) {
-    const double* row = proj->vectors + 12 * (size_t)t;
-    double U[3], V[3], Dc[3], S[3], R[3], ref[3];
-    for (int i = 0; i < 3; ++i) {
-      if (!std::isfinite(row[i]) || !std::isfinite(row[3 + i]) || !std::isfinite(row[6 + i]) ||
-          !std::isfinite(row[9 + i]))
-        return "non-finite geometry vector at angle " + std::to_string(t);
-      const double dc = row[3 + i] + (g->ov + 0.5 - 0.5 * g->rows) * row[6 + i] +
-                        (g->ou + 0.5 - 0.5 * g->cols) * row[9 + i];
-      U[i] = row[9 + i] / vs[i];
-      V[i] = row[6 + i] / vs[i];
-      Dc[i] = (dc - origin[i]) / vs[i];
-      S[i] = (row[i] - origin[i]) / vs[i];
-      R[i] = row[i] / vs[i];
-      ref[i] = cone ? (row[3 + i] - row[i]) / vs[i] : R[i];
-    }
-    const int d = argmax_abs3(ref, -1), b = argmax_abs3(V, d), a = 3 - d - b;
+    tsgb::AngleFrame f;
+    const std::string err = tsgb::reduce_angle(proj->vectors + 12 * (size_t)t, cone, vs, origin,
+                                               g->rows, g->cols, g->ov, g->ou, true, t, &f);
+    if (!err.empty()) return err;
+    const int d = f.d, a = f.a, b = f.b;
     tsgb::AngleParams ap{};
     ap.d = d;
     ap.a = a;
     ap.b = b;
-    double e[3], ca[3], ma[3], cb[3], mb[3];
-    if (cone) {
-      const double D[3] = {Dc[0] - S[0], Dc[1] - S[1], Dc[2] - S[2]};
-      if (D[d] == 0.0) return "detector centre lies in the source's dominant plane";
-      const double sc = 1.0 / D[d];
-      const double ed[3] = {D[d], U[d], V[d]}, ea[3] = {D[a], U[a], V[a]}, eb[3] = {D[b], U[b], V[b]};
-      for (int j = 0; j < 3; ++j) {
-        e[j] = ed[j] * sc;
-        ca[j] = (S[a] * ed[j] - S[d] * ea[j]) * sc;
-        ma[j] = ea[j] * sc;
-        cb[j] = (S[b] * ed[j] - S[d] * eb[j]) * sc;
-        mb[j] = eb[j] * sc;
-      }
-    } else {
-      if (R[d] == 0.0) return "ray parallel to every volume plane";
-      const double sa = R[a] / R[d], sb = R[b] / R[d];
-      e[0] = 1.0;
-      e[1] = e[2] = 0.0;
-      ca[0] = Dc[a] - Dc[d] * sa;
-      ca[1] = U[a] - U[d] * sa;
-      ca[2] = V[a] - V[d] * sa;
-      cb[0] = Dc[b] - Dc[d] * sb;
-      cb[1] = U[b] - U[d] * sb;
-      cb[2] = V[b] - V[d] * sb;
-      ma[0] = sa;
-      mb[0] = sb;
-      ma[1] = ma[2] = mb[1] = mb[2] = 0.0;
-    }
     for (int j = 0; j < 3; ++j) {
-      ap.e[j] = float(e[j]);
-      ap.ca[j] = float(ca[j]);
-      ap.ma[j] = float(ma[j]);
-      ap.cb[j] = float(cb[j]);
-      ap.mb[j] = float(mb[j]);
+      ap.e[j] = float(f.e[j]);
+      ap.ca[j] = float(f.ca[j]);
+      ap.ma[j] = float(f.ma[j]);
+      ap.cb[j] = float(f.cb[j]);
+      ap.mb[j] = float(f.mb[j]);
     }
     int li = -1;
     for (int l = 0; l < *n_layouts; ++l)
@@ -307,11 +287,17 @@ extern "C" int tsgb_direct_fp_noalloc(const tsgb_volume_desc* vol,
   cudaStream_t stream = static_cast<cudaStream_t>(stream_);
   float* scratch = static_cast<float*>(g_scratch_ptr[dev]);
   tsgb::AngleParams* params = static_cast<tsgb::AngleParams*>(g_params_ptr[dev]);
-  // Pageable source: the copy is staged before cudaMemcpyAsync returns, so the
-  // host buffer may be rewritten by the next call.
-  e = cudaMemcpyAsync(params, g_host_params, sizeof(tsgb::AngleParams) * g.nangles,
-                      cudaMemcpyHostToDevice, stream);
-  if (e != cudaSuccess) return fail(TSGB_ERR_CUDA, std::string("parameter upload: ") + cudaGetErrorString(e));
+  // Parameters as kernel arguments: the launch copies each chunk, so
+  // g_host_params is free again as soon as the launch returns.
+  for (int t0 = 0; t0 < g.nangles; t0 += kParamChunk) {
+    const int count = std::min(kParamChunk, g.nangles - t0);
+    ParamChunk chunk;
+    std::memcpy(chunk.p, g_host_params + t0, sizeof(tsgb::AngleParams) * count);
+    noalloc_params_kernel<<<1, 256, 0, stream>>>(chunk, count, params + t0);
+  }
+  e = cudaGetLastError();
+  if (e != cudaSuccess)
+    return fail(TSGB_ERR_CUDA, std::string("parameter upload: ") + cudaGetErrorString(e));
   const int shape[3] = {g.nz, g.ny, g.nx};
   const long long vstride[3] = {(long long)g.ny * g.nx, (long long)g.nx, 1};
   for (int l = 0; l < n_layouts; ++l) {
