@@ -95,6 +95,23 @@ int tsgb_direct_bp(tsgb_projector* p, float* vol, const float* sino,
                    int32_t additive, int32_t bp_kind, void* workspace,
                    int64_t workspace_bytes, void* stream);
 
+/* Forward projection of n volumes stored back to back (item i at
+ * vol + i * Nz*Ny*Nx) into n sinograms (sino + i * rows*num_angles*cols), each
+ * as tsgb_direct_fp, in one call; one workspace of tsgb_fp_workspace_bytes
+ * serves every item (the projections run one after another on ``stream``).
+ * Replaces the per-slice loop over batch and channel dimensions of tomosipo's
+ * to_autograd (tomosipo/torch_support.py:49-53). */
+int tsgb_direct_fp_batch(tsgb_projector* p, const float* vol, float* sino, int64_t n,
+                         int32_t additive, void* workspace, int64_t workspace_bytes,
+                         void* stream);
+
+/* Backprojection of n sinograms into n volumes, laid out as for
+ * tsgb_direct_fp_batch, each as tsgb_direct_bp. Replaces the per-slice loop
+ * of to_autograd's backward pass (tomosipo/torch_support.py:70-74). */
+int tsgb_direct_bp_batch(tsgb_projector* p, float* vol, const float* sino, int64_t n,
+                         int32_t additive, int32_t bp_kind, void* workspace,
+                         int64_t workspace_bytes, void* stream);
+
 /* Forward projection of the angles angle_begin .. angle_end - 1 only, into
  * their slices of the full sinogram (other angles untouched). With
  * copies_ready != 0 the padded volume copies a previous call on the same
@@ -129,11 +146,13 @@ int tsgb_copy_sino_angles(void* dst, const void* src, int64_t rows, int64_t num_
  * and the per-angle parameters -- in fixed static device arrays: at most
  * 16,777,216 floats (64 MiB) of copies (sum of n_d * (n_a + 4) * (n_b + 4) over
  * the axis permutations used; two copies of a 160^3 volume fit) and at most
- * 4096 angles; larger requests fail with TSGB_ERR_INVALID. The first call on
- * each device resolves the arrays' addresses (make it before any stream
- * capture); the arrays then stay allocated on that device until exit. Calls
- * share the arrays, so calls that overlap on the GPU race: keep them on one
- * stream. No counterpart in the reference (tomosipo / ASTRA). */
+ * 4096 angles; larger requests fail with TSGB_ERR_INVALID, as do degenerate
+ * detectors (the regular projector's checks). The first call on each device
+ * resolves the arrays' addresses (make it before any stream capture); the
+ * arrays then stay allocated on that device until exit. Calls share the
+ * arrays, so calls that overlap on the GPU race: keep them on one stream. The
+ * per-angle parameters travel to the device as kernel arguments: a call issues
+ * no host-to-device memcpy. No counterpart in the reference (tomosipo / ASTRA). */
 int tsgb_direct_fp_noalloc(const tsgb_volume_desc* vol, const tsgb_projection_desc* proj,
                            const float* vol_in, float* sino_out, int32_t additive,
                            void* stream);

@@ -129,6 +129,8 @@ _NULL_CALLS = {
     "tsgb_projector_stats": (None, None, 8),
     "tsgb_projector_get_tuning": (None, None),
     "tsgb_projector_set_tuning": (None, None),
+    "tsgb_direct_fp_batch": (None, None, None, 2, 0, None, 0, None),
+    "tsgb_direct_bp_batch": (None, None, None, 2, 0, 0, None, 0, None),
     "tsgb_direct_fp_angles": (None, None, None, 0, 0, 1, 0, None, 0, None),
     "tsgb_direct_bp_angles": (None, None, None, 0, 0, 1, None, 0, None),
     "tsgb_copy_sino_angles": (None, None, 1, 1, 1, 0, 1, None),

@@ -18,7 +18,7 @@ from . import vector_calc as vc
 from .geometry import VolumeGeometry, VolumeVectorGeometry, volume, from_perspective
 from .Data import Data, data
 from .links.base import link, geometry_shape
-from .projector import create_projector, direct_fp, direct_bp, BP_KINDS
+from .projector import create_projector, direct_fp, direct_bp, direct_project_batch, BP_KINDS
 
 
 def to_astra_compatible_operator_geometry(vg, pg):
@@ -133,6 +133,15 @@ class Operator:
         """Forward project ``volume``; writes into ``out`` when given."""
         return self._fp(volume, out)
 
+    def _apply_batch(self, volumes, out):
+        """out[i] = A(volumes[i]) (or += when additive) for stacked CUDA float32
+        tensors (n, z, y, x) -> (n, rows, angles, cols), in one C-ABI call."""
+        direct_project_batch(self.projector, volumes, out, forward=True, additive=self.additive)
+
+    def _bp_batch(self, projections, out):
+        direct_project_batch(self.projector, out, projections, forward=False,
+                             additive=self.additive, bp_kind=self.backprojector)
+
     def transpose(self):
         return self._transpose
 
@@ -165,6 +174,10 @@ class BackprojectionOperator:
 
     def __call__(self, projection, out=None):
         return self.parent._bp(projection, out)
+
+    def _apply_batch(self, projections, out):
+        """out[i] = A.T(projections[i]) for stacked CUDA float32 tensors, in one C-ABI call."""
+        self.parent._bp_batch(projections, out)
 
     def transpose(self):
         return self.parent

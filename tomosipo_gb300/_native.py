@@ -102,6 +102,16 @@ SIGNATURES = {
     "tsgb_sirt_batch_destroy": (ctypes.c_int, [ctypes.c_void_p]),
     "tsgb_projector_get_tuning": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(Tuning)]),
     "tsgb_projector_set_tuning": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(Tuning)]),
+    "tsgb_direct_fp_batch": (
+        ctypes.c_int,
+        [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64, ctypes.c_int32,
+         ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p],
+    ),
+    "tsgb_direct_bp_batch": (
+        ctypes.c_int,
+        [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64, ctypes.c_int32,
+         ctypes.c_int32, ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p],
+    ),
     "tsgb_direct_fp_angles": (
         ctypes.c_int,
         [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int32, ctypes.c_int64,

@@ -249,6 +249,38 @@ int tsgb_direct_bp(tsgb_projector* p, float* vol, const float* sino, int32_t add
   return TSGB_OK;
 }
 
+int tsgb_direct_fp_batch(tsgb_projector* p, const float* vol, float* sino, int64_t n,
+                         int32_t additive, void* workspace, int64_t workspace_bytes,
+                         void* stream) {
+  g_last_error.clear();
+  if (!p || !vol || !sino || n < 0) return fail(TSGB_ERR_INVALID, "NULL projector or data pointer");
+  const size_t vol_elems = size_t(p->g.nz) * p->g.ny * p->g.nx;
+  const size_t sino_elems = size_t(p->g.rows) * p->g.nangles * p->g.cols;
+  // one workspace serves every item: the projections run one after another on
+  // the stream
+  for (int64_t i = 0; i < n; ++i) {
+    const int rc = tsgb_direct_fp(p, vol + i * vol_elems, sino + i * sino_elems, additive,
+                                  workspace, workspace_bytes, stream);
+    if (rc != TSGB_OK) return rc;
+  }
+  return TSGB_OK;
+}
+
+int tsgb_direct_bp_batch(tsgb_projector* p, float* vol, const float* sino, int64_t n,
+                         int32_t additive, int32_t bp_kind, void* workspace,
+                         int64_t workspace_bytes, void* stream) {
+  g_last_error.clear();
+  if (!p || !vol || !sino || n < 0) return fail(TSGB_ERR_INVALID, "NULL projector or data pointer");
+  const size_t vol_elems = size_t(p->g.nz) * p->g.ny * p->g.nx;
+  const size_t sino_elems = size_t(p->g.rows) * p->g.nangles * p->g.cols;
+  for (int64_t i = 0; i < n; ++i) {
+    const int rc = tsgb_direct_bp(p, vol + i * vol_elems, sino + i * sino_elems, additive, bp_kind,
+                                  workspace, workspace_bytes, stream);
+    if (rc != TSGB_OK) return rc;
+  }
+  return TSGB_OK;
+}
+
 int tsgb_direct_fp_angles(tsgb_projector* p, const float* vol, float* sino, int32_t additive,
                           int64_t angle_begin, int64_t angle_end, int32_t copies_ready,
                           void* workspace, int64_t workspace_bytes, void* stream) {

@@ -214,6 +214,67 @@ def _host_ptr(arr):
     return arr.ctypes.data if isinstance(arr, np.ndarray) else arr.data_ptr()
 
 
+class TransferTimeline:
+    """CUDA-event spans of host-data projections, for measurement.
+
+    While installed with ``record_transfers(timeline)``, every pipelined
+    host-to-host projection records labelled spans on the stream each step
+    runs on: ``vol_h2d``, ``fp`` chunks and ``sino_d2h`` chunks in the forward
+    leg; ``sino_h2d`` chunks, ``bp`` chunks and ``vol_d2h`` in the backward
+    leg; and the whole leg (``fp_leg`` / ``bp_leg``). ``summary()`` (after the
+    device is synchronised) sums each label's milliseconds.
+    """
+
+    def __init__(self):
+        self.spans = []
+
+    def begin(self, label, stream):
+        e = torch.cuda.Event(enable_timing=True)
+        e.record(stream)
+        return (label, e)
+
+    def end(self, token, stream):
+        label, e0 = token
+        e1 = torch.cuda.Event(enable_timing=True)
+        e1.record(stream)
+        self.spans.append((label, e0, e1))
+
+    def summary(self):
+        out = {}
+        for label, e0, e1 in self.spans:
+            out[label] = out.get(label, 0.0) + e0.elapsed_time(e1)
+        return out
+
+
+_timeline = None
+
+
+class record_transfers:
+    """Context manager installing a TransferTimeline for host-data projections."""
+
+    def __init__(self, timeline):
+        self.timeline = timeline
+
+    def __enter__(self):
+        global _timeline
+        self._prev, _timeline = _timeline, self.timeline
+        return self.timeline
+
+    def __exit__(self, *exc):
+        global _timeline
+        _timeline = self._prev
+        return False
+
+
+def _begin(label, stream):
+    return _timeline.begin(label, stream) if _timeline is not None else None
+
+
+def _end(token, stream):
+    if token is not None and _timeline is not None:
+        _timeline.end(token, stream)
+
+
 def _pipelined(projector, forward, additive, bp_kind, src, dst):
     """Both buffers on the host and large enough to hide their transfers."""
     rows, nang, cols = projector.sino_shape
@@ -241,42 +302,61 @@ def _project_pipelined(projector, forward, additive, src, dst, device):
         ws = torch.empty(max(nbytes, 1), dtype=torch.uint8, device=device)
         start = torch.cuda.Event()
         if forward:
+            leg = _begin("fp_leg", comp)
+            t = _begin("vol_h2d", comp)
             d_vol, _ = _as_device_tensor(src, device, copy_in=True)
+            _end(t, comp)
             d_sino, _ = _as_device_tensor(dst, device, copy_in=additive)
             start.record(comp)
             copy.wait_event(start)
             for c in range(chunks):
                 a0, a1 = int(bounds[c]), int(bounds[c + 1])
+                t = _begin("fp", comp)
                 _native.check(lib.tsgb_direct_fp_angles(h, d_vol.data_ptr(), d_sino.data_ptr(),
                                                         int(bool(additive)), a0, a1, int(c > 0),
                                                         ws.data_ptr(), nbytes, comp.cuda_stream),
                               "tsgb_direct_fp_angles")
+                _end(t, comp)
                 done = torch.cuda.Event()
                 done.record(comp)
                 copy.wait_event(done)
+                t = _begin("sino_d2h", copy)
                 _native.check(lib.tsgb_copy_sino_angles(_host_ptr(dst), d_sino.data_ptr(), rows,
                                                         nang, cols, a0, a1, copy.cuda_stream),
                               "tsgb_copy_sino_angles")
+                _end(t, copy)
+            finished = torch.cuda.Event()
+            finished.record(copy)
+            comp.wait_event(finished)
+            _end(leg, comp)
             copy.synchronize()
         else:
+            leg = _begin("bp_leg", comp)
             d_sino = torch.empty((rows, nang, cols), dtype=torch.float32, device=device)
             d_vol, _ = _as_device_tensor(dst, device, copy_in=additive)
             start.record(comp)
             copy.wait_event(start)
             for c in range(chunks):
                 a0, a1 = int(bounds[c]), int(bounds[c + 1])
+                t = _begin("sino_h2d", copy)
                 _native.check(lib.tsgb_copy_sino_angles(d_sino.data_ptr(), _host_ptr(src), rows,
                                                         nang, cols, a0, a1, copy.cuda_stream),
                               "tsgb_copy_sino_angles")
+                _end(t, copy)
                 arrived = torch.cuda.Event()
                 arrived.record(copy)
                 comp.wait_event(arrived)
+                t = _begin("bp", comp)
                 _native.check(lib.tsgb_direct_bp_angles(h, d_vol.data_ptr(), d_sino.data_ptr(),
                                                         int(bool(additive) or c > 0), a0, a1,
                                                         ws.data_ptr(), nbytes, comp.cuda_stream),
                               "tsgb_direct_bp_angles")
+                _end(t, comp)
             target = torch.from_numpy(dst) if isinstance(dst, np.ndarray) else dst
+            t = _begin("vol_d2h", comp)
             target.copy_(d_vol)
+            _end(t, comp)
+            _end(leg, comp)
 
 
 def direct_project(projector, vol_link, proj_link, forward=None, additive=False,
@@ -326,6 +406,36 @@ def direct_project(projector, vol_link, proj_link, forward=None, additive=False,
         # Straight device -> host copy into the caller's buffer (a DMA when it is pinned).
         target = torch.from_numpy(dst) if isinstance(dst, np.ndarray) else dst
         target.copy_(d_dst)
+
+
+def direct_project_batch(projector, vol, sino, forward, additive=False, bp_kind="matched"):
+    """Project item i of ``vol`` (n, z, y, x) to/from item i of ``sino``
+    (n, rows, angles, cols) for every i in one C-ABI call: CUDA float32
+    C-contiguous tensors on one device (no coercion; callers check)."""
+    if bp_kind not in BP_KINDS:
+        raise ValueError(f"bp_kind must be one of {sorted(BP_KINDS)}. Got {bp_kind!r}.")
+    n = vol.shape[0]
+    if (tuple(vol.shape[1:]) != projector.vol_shape or tuple(sino.shape[1:]) != projector.sino_shape
+            or sino.shape[0] != n):
+        raise ValueError(
+            f"Expected volumes (n, {projector.vol_shape}) and sinograms (n, {projector.sino_shape}). "
+            f"Got {tuple(vol.shape)} and {tuple(sino.shape)}.")
+    if vol.device != sino.device or not vol.is_cuda:
+        raise ValueError("batched projection needs both tensors on the same CUDA device")
+    device = vol.device
+    lib = _native.load()
+    with torch.cuda.device(device):
+        h = projector.handle(device.index)
+        stream = torch.cuda.current_stream(device).cuda_stream
+        nbytes = projector.workspace_bytes(device.index, forward, bp_kind)
+        ws = torch.empty(max(nbytes, 1), dtype=torch.uint8, device=device)
+        if forward:
+            rc = lib.tsgb_direct_fp_batch(h, vol.data_ptr(), sino.data_ptr(), n, int(bool(additive)),
+                                          ws.data_ptr(), nbytes, stream)
+        else:
+            rc = lib.tsgb_direct_bp_batch(h, vol.data_ptr(), sino.data_ptr(), n, int(bool(additive)),
+                                          BP_KINDS[bp_kind], ws.data_ptr(), nbytes, stream)
+        _native.check(rc, "tsgb_direct_fp_batch" if forward else "tsgb_direct_bp_batch")
 
 
 def direct_fp(projector, vol_data, proj_data, additive=False):

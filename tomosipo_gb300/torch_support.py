@@ -20,8 +20,20 @@ from .Operator import BackprojectionOperator, operator as make_operator
 
 
 def _apply(op, x, out, extra_dims):
+    """op over every slice of the leading ``extra_dims``. This package's
+    operators take all slices of a CUDA tensor in one batched C-ABI call
+    (tsgb_direct_fp_batch / tsgb_direct_bp_batch); other operators, and host
+    data, go slice by slice as in the reference (torch_support.py:49-53)."""
     if len(extra_dims) == 0:
         op(x, out=out)
+        return
+    batch = getattr(op, "_apply_batch", None)
+    if (batch is not None and x.is_cuda and out.is_cuda and x.dtype == torch.float32
+            and x.is_contiguous() and out.is_contiguous()):
+        n = 1
+        for d in extra_dims:
+            n *= d
+        batch(x.reshape(n, *x.shape[len(extra_dims):]), out.reshape(n, *out.shape[len(extra_dims):]))
         return
     for idx in itertools.product(*[range(n) for n in extra_dims]):
         op(x[idx], out=out[idx])
