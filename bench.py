@@ -565,17 +565,27 @@ def run_ours(args, rank, world, local_rank):
             A.T(yh, out=vh)
         torch.cuda.synchronize()
         barrier()
+        from tomosipo_gb300.projector import TransferTimeline, record_transfers
+
+        timeline = TransferTimeline()
         t0 = time.perf_counter()
         calls = []  # both calls return with their results on the host
-        for _ in range(args.steps):
-            ta = time.perf_counter()
-            A(xh, out=yh)
-            tb = time.perf_counter()
-            A.T(yh, out=vh)
-            calls.append((tb - ta, time.perf_counter() - tb))
+        with record_transfers(timeline):
+            for _ in range(args.steps):
+                ta = time.perf_counter()
+                A(xh, out=yh)
+                tb = time.perf_counter()
+                A.T(yh, out=vh)
+                calls.append((tb - ta, time.perf_counter() - tb))
         torch.cuda.synchronize()
         dt = max_over_ranks(time.perf_counter() - t0, world, device)
         barrier()
+        spans = {k: v / args.steps for k, v in timeline.summary().items()}
+        breakdown = {f"{k}_ms": round(v, 3) for k, v in sorted(spans.items())}
+        # device time of each leg not covered by its kernels: the transfers
+        # (and gaps) the chunked pipeline leaves exposed
+        breakdown["fp_exposed_ms"] = round(spans.get("fp_leg", 0) - spans.get("fp", 0), 3)
+        breakdown["bp_exposed_ms"] = round(spans.get("bp_leg", 0) - spans.get("bp", 0), 3)
         vol_b = 4 * N ** 3
         sino_b = 4 * DET[0] * DET[1] * ANGLES
         e2e = {
@@ -586,6 +596,7 @@ def run_ours(args, rank, world, local_rank):
             "ms_per_step": 1e3 * dt / args.steps,
             "fp_ms": 1e3 * statistics.median(c[0] for c in calls),
             "bp_ms": 1e3 * statistics.median(c[1] for c in calls),
+            "per_step_device_ms": breakdown,
             "path": "ts.operator A(x_host)->y_host, A.T(y_host)->x_host, pinned buffers",
         }
 
@@ -595,21 +606,24 @@ def run_ours(args, rank, world, local_rank):
     peak, peak_kind = measured_peak_hbm()
     bp_avg = statistics.mean(bp_ms) / 1e3
     fp_avg = statistics.mean(fp_ms) / 1e3
-    dom_name, dom_t, dom_key = ("bp_matched (weight pass + separable gather)", bp_avg,
-                                "bp_matched_bytes_per_launch_512")
+    bp_kernel = A.projector.get_tuning(device.index)["bp_kernel"]
+    bp_name = ("bp_matched (column-major weight pass + z-lane gather + transpose)" if bp_kernel
+               else "bp_matched (weight pass + voxel-pair gather)")
+    dom_name, dom_t, dom_key = (bp_name, bp_avg, f"bp_matched_kernel{bp_kernel}_bytes_per_call")
     if fp_avg > bp_avg:
-        dom_name, dom_t, dom_key = ("fp (layout copies + ray kernel)", fp_avg,
-                                    "fp_bytes_per_launch_512")
+        dom_name, dom_t, dom_key = ("fp (layout copies + ray kernel)", fp_avg, "fp_bytes_per_call")
     achieved = BYTES_PER_UPDATE * U / dom_t / 1e9
-    # DRAM bytes per call of the dominant kernel(s) from one 1-pass ncu capture
-    # of this workload (profiles/launch_list_cone512_1024.md); other workloads
-    # have no capture.
-    traffic = None
+    # DRAM bytes per call of the dominant kernels, from the committed summary of
+    # a one-pass ncu capture (gpu__time_duration, dram__bytes_read/write) of
+    # this same workload; other workloads have none.
+    traffic = traffic_source = None
     tpath = os.path.join(ROOT, "profiles", "traffic.json")
     if (N, ANGLES) == (512, 1024) and os.path.exists(tpath):
         try:
             with open(tpath) as f:
-                traffic = json.load(f).get(dom_key)
+                tj = json.load(f)
+            traffic = tj.get(dom_key)
+            traffic_source = tj.get("source") if traffic is not None else None
         except (OSError, ValueError):
             traffic = None
     batched = serving = lpd = bilinear = None
@@ -652,6 +666,7 @@ def run_ours(args, rank, world, local_rank):
             "frac": achieved / peak,
             "peak_kind": peak_kind,
             "traffic": traffic,
+            "traffic_source": traffic_source,
             "algorithmic_bytes": f"{BYTES_PER_UPDATE} B per voxel-angle update x {N}^3 x {ANGLES}",
             "step_frac": BYTES_PER_UPDATE * value * 1e9 / world / peak / 1e9,
         },
