@@ -162,8 +162,10 @@ int tsgb_direct_fp_noalloc(const tsgb_volume_desc* vol, const tsgb_projection_de
  * shaped), sino, R (sinogram shaped), residual (2 * (rows + 4) * angles * cols
  * floats, zeroed by the caller once: the backprojector's row-pair layout with
  * two padding rows above and below the detector), fp_workspace
- * (tsgb_fp_workspace_bytes). The job's angles must all use the separable
- * backprojector (det_v along z: circular and helical geometries). */
+ * (tsgb_fp_workspace_bytes). Any geometry without detector supersampling:
+ * angles whose det_v runs along z (circular and helical scans) take the
+ * separable backprojector with the update fused into its epilogue, others
+ * (tilted detectors) the general one followed by an element-wise update. */
 typedef struct {
   tsgb_projector* projector;
   float* vol;

@@ -82,10 +82,6 @@ int tsgb_sirt_batch_create(const tsgb_sirt_job* jobs, int32_t n_jobs, tsgb_sirt_
       return bfail(TSGB_ERR_INVALID, "job " + std::to_string(i) + " has a NULL pointer");
     if (p->device != dev)
       return bfail(TSGB_ERR_DEVICE, "job " + std::to_string(i) + " belongs to another device");
-    if (p->n_general_bp > 0)
-      return bfail(TSGB_ERR_INVALID, "job " + std::to_string(i) +
-                                         " has angles outside the separable backprojector "
-                                         "(det_v not along z); run it with the plain operator");
     if (p->fine)
       return bfail(TSGB_ERR_INVALID, "job " + std::to_string(i) +
                                          " uses detector supersampling; run it with the plain "

@@ -753,11 +753,55 @@ int launch_bp_matched(const tsgb_projector* p, float* vol, const float* sino, bo
   return int(cudaGetLastError());
 }
 
+namespace {
+
+// vol += C * s elementwise, rounded as the plain recipe's x_tmp *= C; x += x_tmp.
+__global__ void sirt_update_kernel(float* __restrict__ vol, const float* __restrict__ C,
+                                   const float* __restrict__ s, long long n) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x)
+    vol[i] = __fadd_rn(vol[i], __fmul_rn(__ldg(s + i), __ldg(C + i)));
+}
+
+}  // namespace
+
 int launch_bp_sirt(const tsgb_projector* p, float* vol, const float* C, const float* res,
                    float* scratch, void* stream_) {
   cudaStream_t stream = static_cast<cudaStream_t>(stream_);
   const float2* pairs = reinterpret_cast<const float2*>(res);
   const int n_ax = p->n_sep_ax, n_ay = p->n_separable_bp - p->n_sep_ax;
+  const DeviceGeometry& g = p->g;
+  if (p->n_general_bp > 0) {
+    // Angles outside the separable backprojector (tilted detectors): the whole
+    // backprojection goes into a sum volume as launch_bp_matched computes it
+    // (separable passes, then the general kernel adding), and the update is a
+    // separate element-wise pass. scratch holds the sum, then the z-lane
+    // kernel's own scratch (the forward workspace fits both).
+    float* vsum = scratch;
+    bool written = false;
+    if (bp_uses_zlane(p)) {
+      float* volt = reinterpret_cast<float*>(reinterpret_cast<char*>(scratch) + bp_volume_bytes(g));
+      written = launch_bp_zlane_separable(p, 0, n_ax, n_ax, n_ay, res, volt, vsum, 0, nullptr,
+                                          stream);
+    } else {
+      if (n_ax > 0)
+        launch_sep_pass(p, true, p->d_sep_angles, n_ax, kBpSet, pairs, vsum, nullptr, nullptr,
+                        stream);
+      if (n_ay > 0)
+        launch_sep_pass(p, false, p->d_sep_angles + n_ax, n_ay, n_ax > 0 ? kBpAdd : kBpSet, pairs,
+                        vsum, nullptr, nullptr, stream);
+      written = n_ax + n_ay > 0;
+    }
+    const dim3 grid((g.nx + 31) / 32, (g.ny + 3) / 4, g.nz);
+    bp_general_kernel<<<grid, dim3(32, 4), 0, stream>>>(p->d_params, p->d_columns, p->d_gen_angles,
+                                                        p->n_general_bp, pairs, vsum, g,
+                                                        written ? 1 : 0, bp_uses_zlane(p) ? 1 : 0);
+    const long long n = (long long)g.nz * g.ny * g.nx;
+    const long long blocks = (n + 255) / 256;
+    sirt_update_kernel<<<int(blocks < 152LL * 32 ? blocks : 152LL * 32), 256, 0, stream>>>(
+        vol, C, vsum, n);
+    return int(cudaGetLastError());
+  }
   if (bp_uses_zlane(p)) {
     // the residual is column-major; scratch holds the [y][x][z] sum
     launch_bp_zlane_separable(p, 0, n_ax, n_ax, n_ay, res, scratch, vol, 2, C, stream);
