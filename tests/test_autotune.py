@@ -174,3 +174,21 @@ def test_batch_tunes_once_per_job_shape(monkeypatch):
     assert len(runs) == len(set(runs)) == len(tuning) == 3
     rows = [A.projector.tuning["fp_patch_rows"] for A in ops]
     assert rows == [2, 2, 4, 16, 2]  # the three cone 8^3 jobs share the first run
+
+
+def test_backprojector_search_times_every_candidate_once():
+    """``fastest_candidate``: the starting backprojector is timed once, then
+    every other kernel / shape; the fastest wins, ties keep the earlier."""
+    start = dict(DEFAULT, bp_kernel=1, bp_shape=2)
+    seen = []
+
+    def measure(t):
+        seen.append((t["bp_kernel"], t["bp_shape"]))
+        return {(0, 0): 3.0, (1, 4): 1.0, (1, 2): 2.0}.get(seen[-1], 5.0)
+
+    best, best_ms, start_ms, trials = at.fastest_candidate(start, at.BP_CANDIDATES, measure)
+    assert (best["bp_kernel"], best["bp_shape"]) == (1, 4) and best_ms == 1.0 and start_ms == 2.0
+    assert trials == len(at.BP_CANDIDATES) == len(seen) == len(set(seen))
+    assert {k: best[k] for k in DEFAULT} == DEFAULT  # forward settings untouched
+    # every candidate is a valid tuning: kernel 0 or 1, shape 0 .. 6
+    assert all(c["bp_kernel"] in (0, 1) and 0 <= c["bp_shape"] <= 6 for c in at.BP_CANDIDATES)

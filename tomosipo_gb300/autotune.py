@@ -16,8 +16,12 @@ SIRT solver launches each job's tiles in its projector's order, so tuning a
 job's operator tunes its part of the batch.
 
 Every schedule gives bit-identical results: only the order of independent
-tiles changes. Results are cached per geometry (shapes, beam kind and a hash
-of the projection vectors) in memory and, if ``cache_path`` is given, in a
+tiles changes. For operators with the matched backprojector the tuner then
+times the backprojection under every kernel and warp shape it offers
+(``bp_kernel``: voxel-pair threads or z-lane warps; ``bp_shape``: the z-lane
+window x z run x warps per block) and sets the fastest; these change only the
+order of fp32 sums. Results are cached per geometry (shapes, beam kind and a
+hash of the projection vectors) in memory and, if ``cache_path`` is given, in a
 JSON file. No counterpart in the reference, whose ASTRA launch shapes are
 fixed.
 """
@@ -34,6 +38,11 @@ PATCH_COLS = (1, 2, 4, 8, 16)
 # the order in which coordinate descent visits the settings
 SEARCH = (("fp_pair_layout", PAIR_LAYOUT), ("fp_patch_rows", PATCH_ROWS),
           ("fp_group_pairs", GROUP_PAIRS), ("fp_patch_cols", PATCH_COLS))
+
+# Matched backprojectors the tuner times: the voxel-pair kernel and every
+# z-lane warp shape (include/tomosipo_gb300.h, tsgb_tuning.bp_shape).
+BP_CANDIDATES = ({"bp_kernel": 0, "bp_shape": 0},) + tuple(
+    {"bp_kernel": 1, "bp_shape": k} for k in range(7))
 
 _cache = {}
 
@@ -67,6 +76,36 @@ def _time_fp(A, x, y, repeats):
     end.record()
     end.synchronize()
     return start.elapsed_time(end) / repeats
+
+
+def _time_bp(A, y, v, repeats):
+    """Mean CUDA-event time (ms) of ``repeats`` backprojections, after one warm-up."""
+    A.T(y, out=v)
+    start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    start.record()
+    for _ in range(repeats):
+        A.T(y, out=v)
+    end.record()
+    end.synchronize()
+    return start.elapsed_time(end) / repeats
+
+
+def fastest_candidate(start, candidates, measure):
+    """Time ``start`` and then every other candidate (dicts of settings merged
+    into ``start``); a candidate wins only if strictly faster. Returns
+    ``(best, best_ms, start_ms, trials)``."""
+    best = dict(start)
+    best_ms = start_ms = measure(best)
+    trials = 1
+    for c in candidates:
+        cand = dict(best, **c)
+        if all(start.get(k) == v for k, v in c.items()):
+            continue  # the starting point, already timed
+        ms = measure(cand)
+        trials += 1
+        if ms < best_ms:
+            best, best_ms = cand, ms
+    return best, best_ms, start_ms, trials
 
 
 def coordinate_descent(start, measure):
@@ -137,7 +176,24 @@ def autotune(A, device=None, repeats=None, cache_path=None, verbose=False, key=N
         best, best_ms, default_ms, trials = coordinate_descent(proj.get_tuning(dev.index),
                                                                measure)
         proj.set_tuning(dev.index, **best)
-    result = {"tuning": best, "ms": best_ms, "default_ms": default_ms, "trials": trials}
+        result = {"tuning": best, "ms": best_ms, "default_ms": default_ms, "trials": trials}
+        if getattr(A, "backprojector", None) == "matched":
+            v = torch.empty(A.domain_shape, device=dev)
+            first_bp = _time_bp(A, y, v, 1)
+            reps_bp = repeats or max(1, min(8, int(20.0 / max(first_bp, 1e-3))))
+
+            def measure_bp(tuning):
+                proj.set_tuning(dev.index, **tuning)
+                ms = _time_bp(A, y, v, reps_bp)
+                if verbose:
+                    print(f"autotune {key}: {tuning} BP {ms:.3f} ms")
+                return ms
+
+            best, bp_ms, bp_default_ms, bp_trials = fastest_candidate(best, BP_CANDIDATES,
+                                                                      measure_bp)
+            proj.set_tuning(dev.index, **best)
+            result.update(tuning=best, bp_ms=bp_ms, bp_default_ms=bp_default_ms,
+                          bp_trials=bp_trials)
     _cache[key] = result
     if cache_path:
         data = _load_file(cache_path)
