@@ -35,9 +35,12 @@ if ROOT not in sys.path:
     sys.path.insert(0, ROOT)
 
 METRIC = "cone FP+BP GUPS at 512^3/1024 angles"
-# Workloads: the headline one (the metric's) and a small one of the same
-# geometry family for profiler captures (volume 256^3, 360 angles, 256x384).
-WORKLOADS = {"headline": (512, 1024, (512, 768)), "c2": (256, 360, (256, 384))}
+# Workloads: the headline one (the metric's) and small ones of the same
+# geometry family for profiler captures: volume 256^3, 360 angles, 256x384;
+# and the headline's volume and detector with 64 angles over 2 pi, whose
+# kernels run with the headline's per-angle launch shapes.
+WORKLOADS = {"headline": (512, 1024, (512, 768)), "c2": (256, 360, (256, 384)),
+             "cone512_64": (512, 64, (512, 768))}
 N, ANGLES, DET = WORKLOADS["headline"]
 HBM_FALLBACK_GBS = 6800.0
 BYTES_PER_UPDATE = 4  # one fp32 voxel operand per voxel-angle update
@@ -352,9 +355,11 @@ def helical_cone_vec(ts, n, angles, rows, cols, rng, jitter_voxels=0.5):
     return ts.cone_vec(shape=(rows, cols), src_pos=src, det_pos=det, det_v=dv, det_u=du)
 
 
-def bench_serving(torch, ts, device, n_requests=8, rate=20.0, iterations=20, seed=5):
-    """Serving loop over Poisson-arrival SIRT requests on helical cone_vec scans."""
-    from tomosipo_gb300.serving import Request, SirtServer, latency_stats
+def serving_requests(torch, ts, device, n_requests, rate, iterations, seed):
+    """Poisson arrivals (mean ``rate``/s) of SIRT requests on helical cone_vec
+    scans: sides from {128, 256, 384, 512}, 256-1024 angles, detector side x
+    min(1.5 side, 768), noisy data (seeded). Returns (requests, updates)."""
+    from tomosipo_gb300.serving import Request
 
     rng = np.random.default_rng(seed)
     arrivals = np.cumsum(rng.exponential(1.0 / rate, n_requests))
@@ -369,31 +374,60 @@ def bench_serving(torch, ts, device, n_requests=8, rate=20.0, iterations=20, see
         reqs.append(Request(i, A, y, iterations, float(arrivals[i])))
         updates += 2 * n ** 3 * angles * iterations
     torch.cuda.synchronize()
-    # the same requests under the all-jobs-every-step policy, for comparison
-    other = SirtServer(policy="all")
-    st_all = latency_stats(other.run(reqs))
+    return reqs, updates
+
+
+def bench_serving(torch, ts, device, n_requests=64, rate=20.0, iterations=20, seed=5,
+                  stable_requests=16, stable_load=0.5):
+    """Serving loop over Poisson-arrival SIRT requests on helical cone_vec scans.
+
+    First the workload's own arrival rate (20/s, far above what one GPU can
+    serve, so a backlog builds and latency is mostly queueing); the completion
+    rate under that backlog is the server's capacity. Then a second request
+    set arriving at ``stable_load`` x that capacity, where queues stay short."""
+    from tomosipo_gb300.serving import SirtServer, latency_stats
+
+    reqs, updates = serving_requests(torch, ts, device, n_requests, rate, iterations, seed)
     server = SirtServer()  # shortest remaining work first (the default)
     t0 = time.perf_counter()
     res = server.run(reqs)
     wall = time.perf_counter() - t0
     st = latency_stats(res)
+    del reqs, res
+    torch.cuda.empty_cache()
+    capacity = st.get("solves_per_s") or 0.0
+    stable = None
+    if stable_requests and capacity > 0:
+        srate = stable_load * capacity
+        reqs2, _ = serving_requests(torch, ts, device, stable_requests, srate, iterations, seed + 1)
+        st2 = latency_stats(SirtServer().run(reqs2))
+        stable = dict(st2, arrival_rate_per_s=srate,
+                      note=f"{stable_requests} requests of the same mix arriving at "
+                           f"{stable_load} x the measured capacity")
+        del reqs2
+        torch.cuda.empty_cache()
     return {
         "config": f"{n_requests} requests, Poisson arrivals {rate}/s, sides from "
                   "{128,256,384,512}, 256-1024 angles, helical cone_vec (1.5 turns, pitch 0.5) "
                   f"with N(0, 0.5 voxel) source/detector jitter, detector side x min(1.5 side, 768), "
                   f"{iterations} iterations, admission by free HBM (seed {seed})",
+        "n_requests": st.get("n_requests"),
+        "completed": st["completed"],
         "p50_latency_s": st.get("p50_s"),
         "p99_latency_s": st.get("p99_s"),
+        "queue_p50_s": st.get("queue_p50_s"),
+        "queue_p99_s": st.get("queue_p99_s"),
+        "service_p50_s": st.get("service_p50_s"),
+        "service_p99_s": st.get("service_p99_s"),
         "solves_per_s": st.get("solves_per_s"),
-        "completed": st["completed"],
+        "offered_rate_per_s": rate,
+        "offered_load_vs_capacity": rate / capacity if capacity else None,
         "max_concurrent_jobs": server.max_concurrent,
         "steps": server.steps,
         "gups": updates / wall / 1e9,
         "policy": "srpt: per step a work budget of one iteration of the largest job, least "
                   "remaining work first, several iterations for small jobs",
-        "all_jobs_each_step": {"p50_latency_s": st_all.get("p50_s"),
-                               "p99_latency_s": st_all.get("p99_s"),
-                               "solves_per_s": st_all.get("solves_per_s")},
+        "stable_rate": stable,
     }
 
 
@@ -633,7 +667,8 @@ def run_ours(args, rank, world, local_rank):
         lpd = bench_lpd(torch, ts, device)
     if not args.no_sirt:
         batched = bench_batched_sirt(torch, ts, device, n_jobs=args.sirt_jobs)
-        serving = bench_serving(torch, ts, device, n_requests=args.serve_requests)
+        serving = bench_serving(torch, ts, device, n_requests=args.serve_requests,
+                                stable_requests=args.serve_stable_requests)
     cpu = parity = None
     if world == 1 and not args.no_cpu_baseline:
         gups, info = cpu_baseline_sample(keep=True)
@@ -697,9 +732,11 @@ def main():
     p.add_argument("--no-lpd", action="store_true", help="skip the learned primal-dual step")
     p.add_argument("--no-bilinear", action="store_true", help="skip the FP + bilinear BP pair")
     p.add_argument("--sirt-jobs", type=int, default=64)
-    p.add_argument("--serve-requests", type=int, default=8)
+    p.add_argument("--serve-requests", type=int, default=64)
+    p.add_argument("--serve-stable-requests", type=int, default=16)
     p.add_argument("--workload", choices=sorted(WORKLOADS), default="headline",
-                   help="headline = the metric's 512^3/1024 workload; c2 = 256^3/360 (profiling)")
+                   help="headline = the metric's 512^3/1024 workload; c2 = 256^3/360 and "
+                   "cone512_64 = 512^3/64 (profiling)")
     p.add_argument("--fp-copies", choices=["auto", "single", "pairs"], default="auto",
                    help="forward projector's volume copies (tuning fp_pair_layout; auto = the "
                    "projector's default): to profile the headline's single-voxel copies on "

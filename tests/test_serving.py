@@ -139,6 +139,13 @@ def test_latency_stats():
     assert st["p50_s"] == pytest.approx(3.0, abs=0.6)
     assert st["p99_s"] == pytest.approx(5.0, abs=0.1)
     assert st["solves_per_s"] == pytest.approx(2.0)
+    # two run at a time, one step (1 s) each: queueing grows with the backlog,
+    # service stays one step; latency = queueing + service for every request
+    assert st["n_requests"] == 10
+    assert st["service_p50_s"] == pytest.approx(1.0, abs=0.05)
+    assert st["service_p99_s"] == pytest.approx(1.0, abs=0.05)
+    assert st["queue_p50_s"] == pytest.approx(st["p50_s"] - 1.0, abs=0.6)
+    assert st["queue_p99_s"] == pytest.approx(4.0, abs=0.1)
 
 
 def test_srpt_finishes_small_jobs_first_with_the_same_results():

@@ -245,22 +245,33 @@ class SirtServer:
         return [results[r.id] for r in requests]
 
 
+def _percentile(values, p):
+    v = sorted(values)
+    k = (len(v) - 1) * p
+    lo, hi = math.floor(k), math.ceil(k)
+    return v[lo] + (v[hi] - v[lo]) * (k - lo)
+
+
 def latency_stats(results):
-    """p50 / p99 latency (s) and throughput (solves/s) of the completed requests."""
+    """Latency of the completed requests (s): end to end (p50 / p99), split into
+    queueing (arrival to admission) and service (admission to completion);
+    throughput (solves/s over the span from the first arrival to the last
+    completion) and request counts."""
     done = [r for r in results if r.status == "done"]
     if not done:
-        return {"completed": 0}
-    lat = sorted(r.latency for r in done)
-
-    def pct(p):
-        k = (len(lat) - 1) * p
-        lo, hi = math.floor(k), math.ceil(k)
-        return lat[lo] + (lat[hi] - lat[lo]) * (k - lo)
-
+        return {"completed": 0, "n_requests": len(results)}
+    lat = [r.latency for r in done]
+    queue = [r.admitted - r.arrival for r in done]
+    service = [r.finished - r.admitted for r in done]
     span = max(r.finished for r in done) - min(r.arrival for r in done)
     return {
+        "n_requests": len(results),
         "completed": len(done),
-        "p50_s": pct(0.50),
-        "p99_s": pct(0.99),
+        "p50_s": _percentile(lat, 0.50),
+        "p99_s": _percentile(lat, 0.99),
+        "queue_p50_s": _percentile(queue, 0.50),
+        "queue_p99_s": _percentile(queue, 0.99),
+        "service_p50_s": _percentile(service, 0.50),
+        "service_p99_s": _percentile(service, 0.99),
         "solves_per_s": len(done) / span if span > 0 else math.inf,
     }
