@@ -310,16 +310,37 @@ def bench_batched_sirt(torch, ts, device, n_jobs=64, iterations=30, seed=3):
     BatchedSirt([small]).run(1)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
+    plain_each = []
     for A, y in jobs:
+        t1 = time.perf_counter()
         sirt(A, y, iterations)
-    torch.cuda.synchronize()
+        torch.cuda.synchronize()
+        plain_each.append(time.perf_counter() - t1)
     t_plain = time.perf_counter() - t0
-    t0 = time.perf_counter()
-    b = BatchedSirt(jobs)
-    b.run(iterations, graph=True)
-    torch.cuda.synchronize()
-    t_batch = time.perf_counter() - t0
-    b.close()
+
+    def batched(js):
+        t1 = time.perf_counter()
+        b = BatchedSirt(js)
+        b.run(iterations, graph=True)
+        torch.cuda.synchronize()
+        dt = time.perf_counter() - t1
+        b.close()
+        return dt
+
+    t_batch = batched(jobs)
+    # per size class: the small jobs (side <= 128) and the large ones, each
+    # batched on its own, against the same jobs' plain-loop times
+    classes = {}
+    for name, pick in (("side_le_128", lambda A: A.domain_shape[0] <= 128),
+                       ("side_gt_128", lambda A: A.domain_shape[0] > 128)):
+        idx = [i for i, (A, _) in enumerate(jobs) if pick(A)]
+        if not idx:
+            continue
+        tb = batched([jobs[i] for i in idx])
+        tp = sum(plain_each[i] for i in idx)
+        classes[name] = {"jobs": len(idx), "batched_s": tb, "plain_loop_s": tp,
+                         "solves_per_s": len(idx) / tb, "plain_loop_solves_per_s": len(idx) / tp,
+                         "speedup_vs_plain_loop": tp / tb}
     return {
         "config": f"{n_jobs} jobs, sides from {{64,96,128,192,256}}, parallel/cone 50/50, "
                   f"60-720 angles, {iterations} iterations, y = A(x) + N(0, 0.01 max) (seed {seed}); "
@@ -333,7 +354,44 @@ def bench_batched_sirt(torch, ts, device, n_jobs=64, iterations=30, seed=3):
         "autotune_s": t_tune,
         "autotuned_shapes": len(tuning),
         "gups": updates / t_batch / 1e9,
+        "size_classes": classes,
     }
+
+
+def bench_general_bp(torch, ts, device, steps, n=256, angles=360, det=(256, 384)):
+    """FP + matched BP of a scan whose detector is tilted out of the z axis (a
+    cone scan rotated 0.4 rad about (1, 0.3, -0.2)): every angle takes the
+    general backprojector (the forward projector is the same kernel as for any
+    geometry). Volume n^3, ``angles`` angles, detector ``det``."""
+    vg = ts.volume(shape=n, size=1)
+    R = ts.rotate(pos=0, axis=(1.0, 0.3, -0.2), angles=0.4)
+    pg = R * ts.cone(angles=angles, shape=det, size=np.sqrt(2), cone_angle=0.5).to_vec()
+    A = ts.operator(vg, pg)
+    st = A.projector.stats(device.index)
+    x = phantom_gpu(torch, device, n, count=8, seed=6)
+    y = torch.empty(A.range_shape, device=device)
+    v = torch.empty(A.domain_shape, device=device)
+    A(x, out=y)
+    A.T(y, out=v)
+    torch.cuda.synchronize()
+    ev = [[torch.cuda.Event(enable_timing=True) for _ in range(3)] for _ in range(steps)]
+    for e in ev:
+        e[0].record()
+        A(x, out=y)
+        e[1].record()
+        A.T(y, out=v)
+        e[2].record()
+    torch.cuda.synchronize()
+    fp = statistics.mean(e[0].elapsed_time(e[1]) for e in ev)
+    bp = statistics.mean(e[1].elapsed_time(e[2]) for e in ev)
+    U = n ** 3 * angles
+    peak, _ = measured_peak_hbm()
+    return {"config": f"cone {n}^3, {angles} angles, detector {det[0]}x{det[1]}, tilted 0.4 rad "
+                      f"about (1, 0.3, -0.2): {st['general_bp_angles']} of {angles} angles on the "
+                      "general backprojector",
+            "fp_ms": fp, "general_bp_ms": bp,
+            "bp_gups": U / (bp / 1e3) / 1e9, "fp_gups": U / (fp / 1e3) / 1e9,
+            "bp_roofline_frac": BYTES_PER_UPDATE * U / (bp / 1e3) / 1e9 / peak}
 
 
 def helical_cone_vec(ts, n, angles, rows, cols, rng, jitter_voxels=0.5):
@@ -660,9 +718,10 @@ def run_ours(args, rank, world, local_rank):
             traffic_source = tj.get("source") if traffic is not None else None
         except (OSError, ValueError):
             traffic = None
-    batched = serving = lpd = bilinear = None
+    batched = serving = lpd = bilinear = general = None
     if not args.no_bilinear:
         bilinear = bench_bilinear_pair(torch, ts, device, x, args.steps)
+        general = bench_general_bp(torch, ts, device, args.steps)
     if not args.no_lpd:
         lpd = bench_lpd(torch, ts, device)
     if not args.no_sirt:
@@ -712,6 +771,7 @@ def run_ours(args, rank, world, local_rank):
         "serving": serving,
         "learned_primal_dual": lpd,
         "fp_plus_bilinear_bp": bilinear,
+        "tilted_detector_general_bp": general,
         "gpu_launches": args.steps * (stats["fp_launches"] + stats["bp_matched_launches"]),
         "clocks": clock_info,
         "plan": stats,

@@ -129,15 +129,32 @@ __device__ __forceinline__ void clip_planes(float X, float m, float lo, float hi
   }
 }
 
+// Exact floor without the conversion unit (as in the z-lane backprojector):
+// for |q| < 2^22, q + 1.5 * 2^23 rounded toward -inf is floor(q) + 1.5 * 2^23,
+// whose bit pattern is 0x4B400000 + floor(q). The sampled positions stay
+// within a few voxels of the volume, far inside that range.
+constexpr float kFloorMagic = 12582912.0f;
+constexpr int kFloorBits = 0x4B400000;
+
+// floor(q) as a float and as an int, and q - floor(q); identical to floorf.
+struct FloorSplit {
+  float frac;
+  int i;
+};
+__device__ __forceinline__ FloorSplit floor_split(float q) {
+  const float m = __fadd_rd(q, kFloorMagic);
+  return {q - (m - kFloorMagic), __float_as_int(m) - kFloorBits};
+}
+
 // Bilinear sample of plane k from single voxels (four 4-byte taps) ...
 __device__ __forceinline__ float bilinear_sample(const float* __restrict__ base, const Ray& r,
                                                  int k, int stride_d, int stride_a) {
   const float kt = float(k);
   const float qa = fmaf(kt, r.ma, r.Xa);
   const float qb = fmaf(kt, r.mb, r.Xb);
-  const float fa0 = floorf(qa), fb0 = floorf(qb);
-  const float fa = qa - fa0, fb = qb - fb0;
-  const float* p = base + (k * stride_d + (int)fa0 * stride_a + (int)fb0);
+  const FloorSplit sa = floor_split(qa), sb = floor_split(qb);
+  const float fa = sa.frac, fb = sb.frac;
+  const float* p = base + (k * stride_d + sa.i * stride_a + sb.i);
   const float v00 = __ldg(p), v01 = __ldg(p + 1);
   const float v10 = __ldg(p + stride_a), v11 = __ldg(p + stride_a + 1);
   const float left = fmaf(fb, v01 - v00, v00);
@@ -152,9 +169,9 @@ __device__ __forceinline__ float bilinear_sample(const float2* __restrict__ base
   const float kt = float(k);
   const float qa = fmaf(kt, r.ma, r.Xa);
   const float qb = fmaf(kt, r.mb, r.Xb);
-  const float fa0 = floorf(qa), fb0 = floorf(qb);
-  const float fa = qa - fa0, fb = qb - fb0;
-  const float2* p = base + (k * stride_d + (int)fa0 * stride_a + (int)fb0);
+  const FloorSplit sa = floor_split(qa), sb = floor_split(qb);
+  const float fa = sa.frac, fb = sb.frac;
+  const float2* p = base + (k * stride_d + sa.i * stride_a + sb.i);
   const float2 v0 = __ldg(p), v1 = __ldg(p + stride_a);
   const float left = fmaf(fb, v0.y - v0.x, v0.x);
   const float right = fmaf(fb, v1.y - v1.x, v1.x);
