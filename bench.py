@@ -599,6 +599,8 @@ def run_ours(args, rank, world, local_rank):
     A = ts.operator(vg, pg)
     if args.fp_copies != "auto":
         A.projector.set_tuning(device.index, fp_pair_layout=int(args.fp_copies == "pairs"))
+    if args.bp_kernel != "auto":
+        A.projector.set_tuning(device.index, bp_kernel=int(args.bp_kernel == "zlane"))
     x = phantom_gpu(torch, device, N, count=20, seed=2)
     y = torch.empty(A.range_shape, device=device)
     v = torch.empty(A.domain_shape, device=device)
@@ -748,7 +750,8 @@ def run_ours(args, rank, world, local_rank):
         "dtype": "f32",
         "data": "synthetic",
         "config": config(dict({"parallelism": f"replicas x{world}" if world > 1 else "single GPU"},
-                              **({"fp_copies": args.fp_copies} if args.fp_copies != "auto" else {}))),
+                              **({"fp_copies": args.fp_copies} if args.fp_copies != "auto" else {}),
+                              **({"bp_kernel": args.bp_kernel} if args.bp_kernel != "auto" else {}))),
         "fp_ms": statistics.mean(fp_ms),
         "bp_ms": statistics.mean(bp_ms),
         "roofline": {
@@ -801,6 +804,9 @@ def main():
                    help="forward projector's volume copies (tuning fp_pair_layout; auto = the "
                    "projector's default): to profile the headline's single-voxel copies on "
                    "the c2 workload")
+    p.add_argument("--bp-kernel", choices=["auto", "pairs", "zlane"], default="auto",
+                   help="matched backprojector (tuning bp_kernel; auto = the projector's default: "
+                   "z-lane warps from 448 voxels along z): to profile the voxel-pair kernel")
     args = p.parse_args()
     global N, ANGLES, DET
     N, ANGLES, DET = WORKLOADS[args.workload]
