@@ -54,7 +54,7 @@ def test_single_rank_is_identity():
 
 def test_reference_arm_only_on_rank_zero():
     class Args:
-        steps_ref, warmup_ref = 1, 0
+        steps, warmup = 1, 0
 
     assert bench.run_reference(Args(), rank=1, world=2) == 0
 
@@ -75,6 +75,12 @@ def test_reference_arm_prints_the_contract_line():
     assert line["impl"] == "reference" and line["unit"] == "GUPS" and line["value"] > 0
     assert line["higher_is_better"] is True and "workload" in line["config"]
     assert line["steps"] == 2 and line["warmup"] == 1  # the counts it ran
+    # the same config the GPU arm reports for this workload on one GPU
+    bench.N, bench.ANGLES, bench.DET = bench.WORKLOADS["c2"]
+    try:
+        assert line["config"] == bench.config({"parallelism": "single GPU"})
+    finally:
+        bench.N, bench.ANGLES, bench.DET = bench.WORKLOADS["headline"]
     cb = line["cpu_baseline"]
     assert cb["kind"] == "port" and cb["cores"] >= 1 and cb["value"] == line["value"] and cb["sample"]
     e2e = line["e2e"]
