@@ -192,12 +192,15 @@ __device__ __forceinline__ void bp_sep_accumulate(const AngleParams* __restrict_
         // end). Two loops behind a per-column branch (nearly every column is
         // inside) beat one loop with predicated clamps by 14 %.
         const bool inside = fminf(vs0, vs1) >= vmin && fmaxf(vs0, vs1) < vmax + 1.0f;
+        // floors by kFloorMagic (no conversion unit); clamping t to the
+        // integers [vmin, vmax] clamps its floor (NaN -> vmin)
         if (inside) {
 #pragma unroll
           for (int j = 0; j < kRun; ++j) {
-            const float v0 = floorf(fmaf(float(j), inv, vs0));
+            const float f = __fadd_rd(fmaf(float(j), inv, vs0), kFloorMagic);
+            const float v0 = f - kFloorMagic;
             const float at0 = fabsf(fmaf(v0, Sl, C0) - float(j));
-            const float2 yy = __ldg(row_at(colv, (int)v0, rs_bytes));
+            const float2 yy = __ldg(row_at(colv, int(__float_as_uint(f) - kFloorBits), rs_bytes));
             const float V = fmaf(__saturatef(1.0f - at0), yy.x, __saturatef(c1s + at0) * yy.y);
 #pragma unroll
             for (int m = 0; m < kA; ++m) acc[m][j] = fmaf(h[m], V, acc[m][j]);
@@ -205,9 +208,11 @@ __device__ __forceinline__ void bp_sep_accumulate(const AngleParams* __restrict_
         } else {
 #pragma unroll
           for (int j = 0; j < kRun; ++j) {
-            const float v0 = fminf(fmaxf(floorf(fmaf(float(j), inv, vs0)), vmin), vmax);
+            const float t = fminf(fmaxf(fmaf(float(j), inv, vs0), vmin), vmax);
+            const float f = __fadd_rd(t, kFloorMagic);
+            const float v0 = f - kFloorMagic;
             const float at0 = fabsf(fmaf(v0, Sl, C0) - float(j));
-            const float2 yy = __ldg(row_at(colv, (int)v0, rs_bytes));
+            const float2 yy = __ldg(row_at(colv, int(__float_as_uint(f) - kFloorBits), rs_bytes));
             const float V = fmaf(__saturatef(1.0f - at0), yy.x, __saturatef(c1s + at0) * yy.y);
 #pragma unroll
             for (int m = 0; m < kA; ++m) acc[m][j] = fmaf(h[m], V, acc[m][j]);

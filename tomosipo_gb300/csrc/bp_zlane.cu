@@ -43,12 +43,6 @@ namespace {
 
 constexpr float kMaxSlopeZ = 64.0f;  // must match fp.cu
 
-// Exact floor without the conversion unit: for |t| < 2^22, t + 1.5 * 2^23
-// rounded toward -inf is floor(t) + 1.5 * 2^23, an integer-valued float whose
-// bit pattern is 0x4B400000 + floor(t) (the spacing of floats there is 1).
-constexpr float kFloorMagic = 12582912.0f;
-constexpr unsigned kFloorBits = 0x4B400000u;
-
 // W * y of pixel (iv, iu) at angle theta, 0 off the detector and for rays the
 // forward projector does not sample.
 __device__ __forceinline__ float weighted_pixel_z(const AngleParams& ap, const ColumnEntry& ce,

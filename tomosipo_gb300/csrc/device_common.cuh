@@ -75,6 +75,15 @@ __device__ __forceinline__ float ray_step(const AngleParams& ap, const Ray& r) {
 
 __device__ __forceinline__ float tent(float t) { return fmaxf(0.0f, 1.0f - fabsf(t)); }
 
+// Exact floor without the conversion unit: for |t| < 2^22, t + 1.5 * 2^23
+// rounded toward -inf (__fadd_rd) is floor(t) + 1.5 * 2^23, an integer-valued
+// float (floats there are spaced by 1) whose bit pattern is 0x4B400000 +
+// floor(t). So floor(t) as a float is that sum minus kFloorMagic, and as an
+// integer its bits minus kFloorBits: add and integer instructions, where
+// floorf plus a float-to-int conversion would occupy the conversion (XU) pipe.
+constexpr float kFloorMagic = 12582912.0f;
+constexpr unsigned kFloorBits = 0x4B400000u;
+
 // Clamp a detector coordinate to +-1e8 before an int conversion (NaN -> -1e8,
 // +-inf -> +-1e8), so range bounds never overflow 32-bit integers.
 __device__ __forceinline__ float clamp_coord(float c) { return fminf(fmaxf(c, -1.0e8f), 1.0e8f); }

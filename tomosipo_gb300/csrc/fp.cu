@@ -129,21 +129,16 @@ __device__ __forceinline__ void clip_planes(float X, float m, float lo, float hi
   }
 }
 
-// Exact floor without the conversion unit (as in the z-lane backprojector):
-// for |q| < 2^22, q + 1.5 * 2^23 rounded toward -inf is floor(q) + 1.5 * 2^23,
-// whose bit pattern is 0x4B400000 + floor(q). The sampled positions stay
-// within a few voxels of the volume, far inside that range.
-constexpr float kFloorMagic = 12582912.0f;
-constexpr int kFloorBits = 0x4B400000;
-
-// floor(q) as a float and as an int, and q - floor(q); identical to floorf.
+// floor(q) as an int and q - floor(q), without the conversion unit
+// (kFloorMagic); identical to floorf. The sampled positions stay within a few
+// voxels of the volume, far inside its |q| < 2^22 range.
 struct FloorSplit {
   float frac;
   int i;
 };
 __device__ __forceinline__ FloorSplit floor_split(float q) {
   const float m = __fadd_rd(q, kFloorMagic);
-  return {q - (m - kFloorMagic), __float_as_int(m) - kFloorBits};
+  return {q - (m - kFloorMagic), int(__float_as_uint(m) - kFloorBits)};
 }
 
 // Bilinear sample of plane k from single voxels (four 4-byte taps) ...
