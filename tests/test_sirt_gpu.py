@@ -90,6 +90,35 @@ def test_batched_graph_replay_equals_eager(dev):
     assert torch.equal(eager.x[3], sirt(jobs[3][0], jobs[3][1], 13))
 
 
+def test_batched_multi_job_groups_equal_plain(dev):
+    """More small jobs than one multi-job launch takes (two groups of one copy
+    layout, one group of the other, a single job of a third kind) beside a job
+    too large to join them; per-job iteration counts, some zero, so groups
+    shrink between iterations. Every job equals the plain SIRT loop bit for bit."""
+    from tomosipo_gb300.sirt import NativeBatch, SirtJobState
+
+    jobs = []
+    for i in range(53):
+        n = (8, 12, 16, 20)[i % 4]
+        A, y, _ = _job(dev, n, i % 3 != 0, 4 + (i * 7) % 13, 100 + i)
+        if i >= 45:  # single-voxel copies: the other multi-job kernel
+            A.projector.set_tuning(dev.index, fp_pair_layout=0)
+        jobs.append((A, y))
+    # a volume above 2^21 voxels keeps its own launches
+    vg = ts.volume(shape=(130, 128, 128), size=(130 / 128, 1, 1))
+    pg = ts.cone(angles=5, shape=(130, 192), size=(130 / 128 * np.sqrt(2), 1.5), cone_angle=0.5)
+    A = ts.operator(vg, pg)
+    jobs.append((A, A(torch.from_numpy(ellipsoid_phantom(vg.shape, n=4, seed=7)).to(dev))))
+    counts = [(i * 5) % 4 for i in range(len(jobs))]
+    states = [SirtJobState(A, y, None, dev) for A, y in jobs]
+    nb = NativeBatch(states)
+    nb.step_jobs(counts)
+    torch.cuda.synchronize()
+    for (A, y), st, k in zip(jobs, states, counts):
+        assert torch.equal(st.x, sirt(A, y, k)), (A.domain_shape, k)
+    nb.close()
+
+
 def test_batched_tilted_detectors_equal_plain(dev):
     """Tilted detectors (the general backprojector), alone and beside a
     circular scan, on both matched backprojectors for the separable angles:

@@ -8,16 +8,22 @@
 // forward projection writes the residual W * R * (y - A x) straight into the
 // backprojector's row-pair layout, and the backprojection applies
 // x += C * A^T(res), so one iteration of one job is its padded volume copies
-// plus two kernels, with no element-wise passes. Jobs are spread over a small
-// pool of streams (largest first, round robin), forked from and joined back
-// into the caller's stream: small jobs run beside large ones and fill the SMs
-// a single small launch would leave idle. Under stream capture the fork and
-// join become a CUDA graph with one branch per stream.
+// plus two kernels, with no element-wise passes.
 //
-// One fused launch over all jobs was the earlier design; it read each job's
-// geometry from a device table, and the registers that cost (values the
-// per-job kernels take from the parameter bank) made large jobs ~15 % slower
-// than running them alone, which outweighed the gain on small jobs.
+// Small jobs (at most 128^3 voxels, voxel-pair backprojector, no tilted
+// detectors) are grouped, up to kMaxMultiJobs at a time, into multi-job
+// launches: one forward launch and one launch per backprojection pass cover
+// the whole group, each block running one tile of one job exactly as that
+// job's own launch would (the job descriptors travel as __grid_constant__
+// kernel arguments, so the per-job kernels keep their registers). A small
+// job's backprojection alone fills a fraction of the SMs for a time set by its
+// angle count, whatever its volume; in a group its blocks queue behind the
+// others' and the SMs stay busy. Larger jobs keep their own launches.
+//
+// Work units (a large job, or a group of small ones) are spread over a small
+// pool of streams (largest first, round robin), forked from and joined back
+// into the caller's stream, so units run beside each other. Under stream
+// capture the fork and join become a CUDA graph with one branch per stream.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -33,6 +39,25 @@ namespace {
 // Streams per batch: at most the default number of hardware queues
 // (CUDA_DEVICE_MAX_CONNECTIONS = 8), so streams never share a queue.
 constexpr int kMaxStreams = 8;
+// Jobs of at most this many voxels (128^3) join multi-job launches.
+constexpr long long kMultiMaxVoxels = 1LL << 21;
+
+// A stream's unit of work: one job on its own launches, or a group of small
+// jobs of one copy layout on multi-job launches.
+struct Unit {
+  std::vector<int> jobs;  // indices into the batch's (sorted) jobs
+  bool multi = false;
+  bool pair_layout = false;
+  double work = 0.0;
+};
+
+bool multi_eligible(const tsgb_projector* p) {
+  const tsgb::DeviceGeometry& g = p->g;
+  int gx = 0, gy = 0;
+  return (long long)g.nz * g.ny * g.nx <= kMultiMaxVoxels && !tsgb::bp_uses_zlane(p) &&
+         p->n_general_bp == 0 && tsgb::fp_multi_eligible(p) &&
+         tsgb::bp_sep_blocks(p, true, &gx, &gy) >= 0;
+}
 
 int bfail(int code, const std::string& msg) {
   tsgb::set_last_error(msg);
@@ -45,6 +70,7 @@ struct tsgb_sirt_batch {
   int device = -1;
   std::vector<tsgb_sirt_job> jobs;  // largest first
   std::vector<int> index;           // jobs[k] is the caller's job index[k]
+  std::vector<Unit> units;          // largest first; unit u runs on stream u % streams
   std::vector<cudaStream_t> streams;
   std::vector<cudaEvent_t> joins;
   cudaEvent_t fork = nullptr;
@@ -99,8 +125,35 @@ int tsgb_sirt_batch_create(const tsgb_sirt_job* jobs, int32_t n_jobs, tsgb_sirt_
     b->jobs.push_back(jobs[i]);
     b->index.push_back(i);
   }
+  // units: each large job alone; the small ones by copy layout, in groups of
+  // at most kMaxMultiJobs (a group of one is a plain unit)
+  std::vector<int> small[2];
+  for (int k = 0; k < n_jobs; ++k) {
+    const tsgb_projector* p = b->jobs[k].projector;
+    if (multi_eligible(p))
+      small[p->tuning.fp_pair_layout ? 1 : 0].push_back(k);
+    else
+      b->units.push_back(Unit{{k}, false, false, work[order[k]]});
+  }
+  for (int layout = 0; layout < 2; ++layout) {
+    const int n = int(small[layout].size());
+    const int groups = (n + tsgb::kMaxMultiJobs - 1) / tsgb::kMaxMultiJobs;
+    for (int q = 0; q < groups; ++q) {
+      Unit u;
+      u.multi = true;
+      u.pair_layout = layout == 1;
+      for (int k = q; k < n; k += groups) {  // groups of near-equal size and work
+        u.jobs.push_back(small[layout][k]);
+        u.work += work[order[small[layout][k]]];
+      }
+      if (u.jobs.size() == 1) u.multi = false;
+      b->units.push_back(u);
+    }
+  }
+  std::stable_sort(b->units.begin(), b->units.end(),
+                   [](const Unit& a, const Unit& c) { return a.work > c.work; });
 
-  const int n_streams = std::min(n_jobs, kMaxStreams);
+  const int n_streams = std::min(int(b->units.size()), kMaxStreams);
   e = cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming);
   for (int k = 0; k < n_streams && e == cudaSuccess; ++k) {
     cudaStream_t s = nullptr;
@@ -123,6 +176,76 @@ int tsgb_sirt_batch_create(const tsgb_sirt_job* jobs, int32_t n_jobs, tsgb_sirt_
 
 namespace {
 
+// One SIRT iteration of job J on its own launches.
+cudaError_t iterate_job(const tsgb_sirt_job& J, cudaStream_t s) {
+  const tsgb::FpSirt sirt{J.sino, J.R, J.residual, tsgb::bp_uses_zlane(J.projector) ? 1 : 0};
+  cudaError_t e = cudaError_t(tsgb::launch_fp(J.projector, J.vol, nullptr, false, J.fp_workspace, s, &sirt));
+  // the forward workspace is free once the residual is written: it holds the
+  // first backprojection pass's sum
+  if (e == cudaSuccess)
+    e = cudaError_t(tsgb::launch_bp_sirt(J.projector, J.vol, J.C, J.residual, J.fp_workspace, s));
+  return e;
+}
+
+// One SIRT iteration of the small jobs `members` on multi-job launches: each
+// job's volume copies, one forward launch, then one launch per backprojection
+// pass; every job's arithmetic is that of iterate_job.
+cudaError_t iterate_group(const std::vector<const tsgb_sirt_job*>& members, bool pair_layout,
+                          cudaStream_t s) {
+  cudaError_t e = cudaSuccess;
+  tsgb::FpMulti fm{};
+  for (const tsgb_sirt_job* J : members) {
+    const tsgb_projector* p = J->projector;
+    e = cudaError_t(tsgb::launch_fp_copies(p, J->vol, J->fp_workspace, s));
+    if (e != cudaSuccess) return e;
+    tsgb::FpMultiJob& F = fm.job[fm.n];
+    F.params = p->d_params;
+    F.columns = p->d_columns;
+    F.ws = J->fp_workspace;
+    F.g = p->g;
+    F.sched = tsgb::fp_schedule(p, (p->g.nangles + 1) / 2);
+    F.sirt = tsgb::FpSirt{J->sino, J->R, J->residual, 0};
+    fm.start[fm.n + 1] = fm.start[fm.n] + tsgb::fp_blocks(p);
+    ++fm.n;
+  }
+  e = cudaError_t(tsgb::launch_fp_multi(fm, pair_layout, s));
+  // Backprojection: the pass along x, then the pass along y (which adds the
+  // first pass's sum from the forward workspace); a job with angles in one
+  // pass only applies its update there. Jobs with more angles (longer blocks)
+  // go first.
+  std::vector<const tsgb_sirt_job*> by_angles(members);
+  std::stable_sort(by_angles.begin(), by_angles.end(),
+                   [](const tsgb_sirt_job* a, const tsgb_sirt_job* c) {
+                     return a->projector->g.nangles > c->projector->g.nangles;
+                   });
+  for (int pass = 0; pass < 2 && e == cudaSuccess; ++pass) {
+    const bool a_is_x = pass == 0;
+    tsgb::BpMulti bm{};
+    for (const tsgb_sirt_job* J : by_angles) {
+      const tsgb_projector* p = J->projector;
+      const int n_ax = p->n_sep_ax, n_ay = p->n_separable_bp - p->n_sep_ax;
+      const int n = a_is_x ? n_ax : n_ay;
+      if (n == 0) continue;
+      const bool both = n_ax > 0 && n_ay > 0;
+      tsgb::BpMultiJob& B = bm.job[bm.n];
+      B.params = p->d_params;
+      B.columns = p->d_columns;
+      B.angles = p->d_sep_angles + (a_is_x ? 0 : n_ax);
+      B.n_angles = n;
+      B.pairs = J->residual;
+      B.vol = J->vol;
+      B.C = J->C;
+      B.scratch = both ? J->fp_workspace : nullptr;
+      B.mode = (a_is_x && both) ? 2 : 3;
+      B.g = p->g;
+      bm.start[bm.n + 1] = bm.start[bm.n] + tsgb::bp_sep_blocks(p, a_is_x, &B.gx, &B.gy);
+      ++bm.n;
+    }
+    e = cudaError_t(tsgb::launch_bp_sep_multi(bm, a_is_x, s));
+  }
+  return e;
+}
+
 // Iterations count[k] of the batch's job k (its sorted order), forked from and
 // joined back into `stream`.
 int iterate_counts(tsgb_sirt_batch* b, const std::vector<int>& count, cudaStream_t stream) {
@@ -133,19 +256,22 @@ int iterate_counts(tsgb_sirt_batch* b, const std::vector<int>& count, cudaStream
   cudaError_t e = cudaEventRecord(b->fork, stream);
   for (int k = 0; k < K && e == cudaSuccess; ++k) e = cudaStreamWaitEvent(b->streams[k], b->fork, 0);
   // Iteration-major submission keeps the streams' queues interleaved; a
-  // job's iterations stay in order on its stream, jobs never wait for each
+  // job's iterations stay in order on its stream, units never wait for each
   // other.
+  std::vector<const tsgb_sirt_job*> members;
   for (int it = 0; it < iterations && e == cudaSuccess; ++it) {
-    for (size_t i = 0; i < b->jobs.size() && e == cudaSuccess; ++i) {
-      if (it >= count[i]) continue;
-      const tsgb_sirt_job& J = b->jobs[i];
-      cudaStream_t s = b->streams[i % K];
-      const tsgb::FpSirt sirt{J.sino, J.R, J.residual, tsgb::bp_uses_zlane(J.projector) ? 1 : 0};
-      e = cudaError_t(tsgb::launch_fp(J.projector, J.vol, nullptr, false, J.fp_workspace, s, &sirt));
-      // the forward workspace is free once the residual is written: it holds
-      // the first backprojection pass's sum
-      if (e == cudaSuccess)
-        e = cudaError_t(tsgb::launch_bp_sirt(J.projector, J.vol, J.C, J.residual, J.fp_workspace, s));
+    for (size_t u = 0; u < b->units.size() && e == cudaSuccess; ++u) {
+      const Unit& U = b->units[u];
+      cudaStream_t s = b->streams[u % K];
+      members.clear();
+      for (int k : U.jobs)
+        if (it < count[k]) members.push_back(&b->jobs[k]);
+      if (members.empty()) continue;
+      if (U.multi && members.size() > 1)
+        e = iterate_group(members, U.pair_layout, s);
+      else
+        for (size_t m = 0; m < members.size() && e == cudaSuccess; ++m)
+          e = iterate_job(*members[m], s);
     }
   }
   for (int k = 0; k < K && e == cudaSuccess; ++k) {

@@ -256,24 +256,26 @@ enum BpSepMode {
 // registers) measured fastest for 2 x 16 voxels per thread: fewer registers
 // spill the accumulators, more cut occupancy. A block of 128 threads is kTA
 // threads along a times 128 / kTA planes, a-fastest, or plane-fastest (kPF).
-template <int kA, int kRun, bool kWide, bool kAisX, int kMode, int kTA, bool kPF>
-__global__ void __launch_bounds__(kBpX* kBpY, 6)
-    bp_separable_kernel(const AngleParams* __restrict__ params,
-                        const ColumnEntry* __restrict__ columns, const int* __restrict__ angles,
-                        int n_angles, const float2* __restrict__ sinow, float* __restrict__ vol,
-                        DeviceGeometry g, const float* __restrict__ C,
-                        float* __restrict__ scratch) {
+template <int kA, int kRun, bool kWide, bool kAisX, int kTA, bool kPF>
+__device__ __forceinline__ void bp_sep_tile(const AngleParams* __restrict__ params,
+                                            const ColumnEntry* __restrict__ columns,
+                                            const int* __restrict__ angles, int n_angles,
+                                            const float2* __restrict__ sinow,
+                                            float* __restrict__ vol, const DeviceGeometry& g,
+                                            const float* __restrict__ C,
+                                            float* __restrict__ scratch, int mode, int bx, int by,
+                                            int bz) {
   constexpr int kTP = kBpX * kBpY / kTA;
   const int t = threadIdx.x;
   const int ta = kPF ? t / kTP : t % kTA;
   const int tp = kPF ? t % kTP : t / kTA;
   // plane-fastest tiles also run their blocks plane-fastest
-  const int ba = kPF ? blockIdx.y : blockIdx.x, bp = kPF ? blockIdx.x : blockIdx.y;
+  const int ba = kPF ? by : bx, bp = kPF ? bx : by;
   const int ia0 = (ba * kTA + ta) * kA;  // first voxel along a
   const int ip = bp * kTP + tp;          // plane
   const int x0 = kAisX ? ia0 : ip;
   const int y0 = kAisX ? ip : ia0;
-  const int z0 = blockIdx.z * kRun;
+  const int z0 = bz * kRun;
   if (x0 >= g.nx || y0 >= g.ny) return;
   const float xt = float(x0 - g.ox), yt = float(y0 - g.oy);
   // a = x: the dominant axis is y (kt = y); a = y: it is x.
@@ -291,11 +293,11 @@ __global__ void __launch_bounds__(kBpX* kBpY, 6)
       const int z = z0 + j;
       if (z >= g.nz) continue;
       const size_t idx = ((size_t)z * g.ny + y) * g.nx + x;
-      if (kMode == kBpSet) {
+      if (mode == kBpSet) {
         vol[idx] = acc[m][j];
-      } else if (kMode == kBpAdd) {
+      } else if (mode == kBpAdd) {
         vol[idx] += acc[m][j];
-      } else if (kMode == kBpSirtFirst) {
+      } else if (mode == kBpSirtFirst) {
         scratch[idx] = acc[m][j];
       } else {
         const float s = scratch ? __fadd_rn(scratch[idx], acc[m][j]) : acc[m][j];
@@ -303,6 +305,34 @@ __global__ void __launch_bounds__(kBpX* kBpY, 6)
       }
     }
   }
+}
+
+template <int kA, int kRun, bool kWide, bool kAisX, int kMode, int kTA, bool kPF>
+__global__ void __launch_bounds__(kBpX* kBpY, 6)
+    bp_separable_kernel(const AngleParams* __restrict__ params,
+                        const ColumnEntry* __restrict__ columns, const int* __restrict__ angles,
+                        int n_angles, const float2* __restrict__ sinow, float* __restrict__ vol,
+                        DeviceGeometry g, const float* __restrict__ C,
+                        float* __restrict__ scratch) {
+  bp_sep_tile<kA, kRun, kWide, kAisX, kTA, kPF>(params, columns, angles, n_angles, sinow, vol, g,
+                                                C, scratch, kMode, blockIdx.x, blockIdx.y,
+                                                blockIdx.z);
+}
+
+// One SIRT pass of many jobs in one launch: block b runs block b - start[j] of
+// job j's grid (gx x gy x z blocks, x fastest) with the job's own epilogue
+// mode, exactly as bp_separable_kernel would for that job alone. 32-bit
+// sinogram offsets only.
+template <int kA, int kRun, bool kAisX, int kTA, bool kPF>
+__global__ void __launch_bounds__(kBpX* kBpY, 6)
+    bp_separable_multi_kernel(const __grid_constant__ BpMulti m) {
+  const int j = multi_job_of(m.start, m.n, blockIdx.x);
+  const BpMultiJob& J = m.job[j];
+  const int local = int(blockIdx.x - m.start[j]);
+  const int bx = local % J.gx, r = local / J.gx;
+  bp_sep_tile<kA, kRun, false, kAisX, kTA, kPF>(
+      J.params, J.columns, J.angles, J.n_angles, reinterpret_cast<const float2*>(J.pairs), J.vol,
+      J.g, J.C, J.scratch, J.mode, bx, r % J.gy, r / J.gy);
 }
 
 __device__ __forceinline__ float coord(int axis, float z, float y, float x) {
@@ -616,17 +646,21 @@ namespace {
 
 constexpr int kSepA = 2;  // voxel columns per thread along a (matched)
 
+// Grid of a pass with kTA threads along a, a-fastest or plane-fastest (kPF).
+dim3 sep_grid(const DeviceGeometry& g, bool a_is_x, int ta, bool pf) {
+  const int tp = kBpX * kBpY / ta;
+  const int n_a = a_is_x ? g.nx : g.ny, n_p = a_is_x ? g.ny : g.nx;
+  const unsigned ga = (n_a + ta * kSepA - 1) / (ta * kSepA), gp = (n_p + tp - 1) / tp;
+  return dim3(pf ? gp : ga, pf ? ga : gp, (g.nz + kRunZ - 1) / kRunZ);
+}
+
 template <bool kWide, bool kAisX, int kMode, int kTA, bool kPF>
 void launch_sep_tile(const tsgb_projector* p, const int* angles, int n, const float2* pairs,
                      float* vol, const float* C, float* scratch, cudaStream_t stream) {
-  const DeviceGeometry& g = p->g;
-  constexpr int kTP = kBpX * kBpY / kTA;
-  const int n_a = kAisX ? g.nx : g.ny, n_p = kAisX ? g.ny : g.nx;
-  const unsigned ga = (n_a + kTA * kSepA - 1) / (kTA * kSepA), gp = (n_p + kTP - 1) / kTP;
-  const dim3 grid(kPF ? gp : ga, kPF ? ga : gp, (g.nz + kRunZ - 1) / kRunZ);
+  const dim3 grid = sep_grid(p->g, kAisX, kTA, kPF);
   bp_separable_kernel<kSepA, kRunZ, kWide, kAisX, kMode, kTA, kPF>
-      <<<grid, kBpX * kBpY, 0, stream>>>(p->d_params, p->d_columns, angles, n, pairs, vol, g, C,
-                                         scratch);
+      <<<grid, kBpX * kBpY, 0, stream>>>(p->d_params, p->d_columns, angles, n, pairs, vol, p->g,
+                                         C, scratch);
 }
 
 // Thread tiles of the two passes (bit-identical results; measured at 512^3 /
@@ -635,13 +669,18 @@ void launch_sep_tile(const tsgb_projector* p, const int* angles, int n, const fl
 // share, 2.6 % faster than 32 pairs along x (68 columns). a = y: a warp is 32
 // planes (x) of one voxel pair along y, plane-fastest, which also keeps the
 // stores along x contiguous; tiles with 8 or 16 planes were slower.
+constexpr int kTileAx = 8, kTileAy = 4;  // threads along a of the two passes
+constexpr bool kPlaneFastAx = false, kPlaneFastAy = true;
+
 template <bool kWide, bool kAisX, int kMode>
 void launch_sep_pass_t(const tsgb_projector* p, const int* angles, int n, const float2* pairs,
                        float* vol, const float* C, float* scratch, cudaStream_t stream) {
   if constexpr (kAisX)
-    launch_sep_tile<kWide, kAisX, kMode, 8, false>(p, angles, n, pairs, vol, C, scratch, stream);
+    launch_sep_tile<kWide, kAisX, kMode, kTileAx, kPlaneFastAx>(p, angles, n, pairs, vol, C,
+                                                                scratch, stream);
   else
-    launch_sep_tile<kWide, kAisX, kMode, 4, true>(p, angles, n, pairs, vol, C, scratch, stream);
+    launch_sep_tile<kWide, kAisX, kMode, kTileAy, kPlaneFastAy>(p, angles, n, pairs, vol, C,
+                                                                scratch, stream);
 }
 
 template <bool kWide, bool kAisX>
@@ -665,15 +704,18 @@ void launch_sep_pass_m(const tsgb_projector* p, const int* angles, int n, int mo
 
 // One pass of the separable matched backprojection over the n angle ids at
 // `angles` (device), all with in-plane axis x (a_is_x) or all with y.
+// 32-bit offsets need fewer than 2^31 padded pairs and a row stride below
+// 2^31 bytes
+bool sep_wide(const DeviceGeometry& g) {
+  const size_t rs = (size_t)g.nangles * g.cols;
+  return (size_t)(g.rows + 2 * kRowPad) * rs >= (size_t(1) << 31) ||
+         rs * sizeof(float2) >= (size_t(1) << 31);
+}
+
 void launch_sep_pass(const tsgb_projector* p, bool a_is_x, const int* angles, int n, int mode,
                      const float2* pairs, float* vol, const float* C, float* scratch,
                      cudaStream_t stream) {
-  const DeviceGeometry& g = p->g;
-  // 32-bit offsets need fewer than 2^31 padded pairs and a row stride below
-  // 2^31 bytes
-  const size_t rs = (size_t)g.nangles * g.cols;
-  const bool wide = (size_t)(g.rows + 2 * kRowPad) * rs >= (size_t(1) << 31) ||
-                    rs * sizeof(float2) >= (size_t(1) << 31);
+  const bool wide = sep_wide(p->g);
   if (wide && a_is_x)
     launch_sep_pass_m<true, true>(p, angles, n, mode, pairs, vol, C, scratch, stream);
   else if (wide)
@@ -822,6 +864,28 @@ int launch_bp_sirt(const tsgb_projector* p, float* vol, const float* C, const fl
   } else if (n_ay > 0) {
     launch_sep_pass(p, false, ay, n_ay, kBpSirtLast, pairs, vol, C, nullptr, stream);
   }
+  return int(cudaGetLastError());
+}
+
+long long bp_sep_blocks(const tsgb_projector* p, bool a_is_x, int* gx, int* gy) {
+  if (sep_wide(p->g)) return -1;
+  const dim3 grid = a_is_x ? sep_grid(p->g, true, kTileAx, kPlaneFastAx)
+                           : sep_grid(p->g, false, kTileAy, kPlaneFastAy);
+  *gx = int(grid.x);
+  *gy = int(grid.y);
+  return (long long)grid.x * grid.y * grid.z;
+}
+
+int launch_bp_sep_multi(const BpMulti& m, bool a_is_x, void* stream_) {
+  cudaStream_t stream = static_cast<cudaStream_t>(stream_);
+  const long long blocks = m.start[m.n];
+  if (blocks <= 0) return int(cudaGetLastError());
+  if (a_is_x)
+    bp_separable_multi_kernel<kSepA, kRunZ, true, kTileAx, kPlaneFastAx>
+        <<<unsigned(blocks), kBpX * kBpY, 0, stream>>>(m);
+  else
+    bp_separable_multi_kernel<kSepA, kRunZ, false, kTileAy, kPlaneFastAy>
+        <<<unsigned(blocks), kBpX * kBpY, 0, stream>>>(m);
   return int(cudaGetLastError());
 }
 

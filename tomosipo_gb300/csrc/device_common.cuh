@@ -73,6 +73,20 @@ __device__ __forceinline__ float ray_step(const AngleParams& ap, const Ray& r) {
   return sqrtf(fmaf(vd, vd, fmaf(va, va, vb * vb)));
 }
 
+// Job of block b in a multi-job launch: the j with start[j] <= b < start[j + 1]
+// (start[0] = 0, n jobs).
+__device__ __forceinline__ int multi_job_of(const long long* start, int n, long long b) {
+  int lo = 0, hi = n;
+  while (hi - lo > 1) {
+    const int mid = (lo + hi) >> 1;
+    if (b >= start[mid])
+      lo = mid;
+    else
+      hi = mid;
+  }
+  return lo;
+}
+
 __device__ __forceinline__ float tent(float t) { return fmaxf(0.0f, 1.0f - fabsf(t)); }
 
 // Exact floor without the conversion unit: for |t| < 2^22, t + 1.5 * 2^23

@@ -345,14 +345,19 @@ __device__ __forceinline__ void sirt_residual(const FpSirt& s, const DeviceGeome
 // registers a thread, which the plane loop spends on loads in flight.
 // kSirt: write the SIRT residual (sirt_residual) instead of the sinogram.
 // E: the copies' element type (float: single voxels, float2: pairs along b).
+// One tile (the schedule's block `block`) of the forward projection; the body
+// of fp_ray_kernel and of fp_ray_multi_kernel. out_slot: the block's shared
+// parking slots (one per thread).
 template <bool kSirt, typename E>
-__global__ void __launch_bounds__(kFpRows* kFpCols, 4)
-    fp_ray_kernel(const AngleParams* __restrict__ params, const ColumnEntry* __restrict__ columns,
-                  const E* __restrict__ ws, float* __restrict__ sino, DeviceGeometry g,
-                  FpSchedule sched, int angle0, int angle_end, int additive, FpSirt sirt) {
-  __shared__ volatile long long out_slot[kFpRows * kFpCols];
+__device__ __forceinline__ void fp_ray_tile(const AngleParams* __restrict__ params,
+                                            const ColumnEntry* __restrict__ columns,
+                                            const E* __restrict__ ws, float* __restrict__ sino,
+                                            const DeviceGeometry& g, const FpSchedule& sched,
+                                            int angle0, int angle_end, int additive,
+                                            const FpSirt& sirt, long long block,
+                                            volatile long long* out_slot) {
   int rb, cb, pr;
-  fp_schedule_tile(sched, blockIdx.x, rb, cb, pr);
+  fp_schedule_tile(sched, block, rb, cb, pr);
   const int iv = rb * kFpRows + threadIdx.x;
   const int iu = cb * kFpCols + threadIdx.y;
   const int theta = angle0 + 2 * pr;
@@ -384,6 +389,28 @@ __global__ void __launch_bounds__(kFpRows* kFpCols, 4)
       if (pair) out[g.cols] = tb;
     }
   }
+}
+
+template <bool kSirt, typename E>
+__global__ void __launch_bounds__(kFpRows* kFpCols, 4)
+    fp_ray_kernel(const AngleParams* __restrict__ params, const ColumnEntry* __restrict__ columns,
+                  const E* __restrict__ ws, float* __restrict__ sino, DeviceGeometry g,
+                  FpSchedule sched, int angle0, int angle_end, int additive, FpSirt sirt) {
+  __shared__ volatile long long out_slot[kFpRows * kFpCols];
+  fp_ray_tile<kSirt, E>(params, columns, ws, sino, g, sched, angle0, angle_end, additive, sirt,
+                        blockIdx.x, out_slot);
+}
+
+// SIRT forward projections of many jobs in one launch: block b runs tile
+// b - start[j] of job j, exactly as fp_ray_kernel would for that job alone.
+template <typename E>
+__global__ void __launch_bounds__(kFpRows* kFpCols, 4)
+    fp_ray_multi_kernel(const __grid_constant__ FpMulti m) {
+  __shared__ volatile long long out_slot[kFpRows * kFpCols];
+  const int j = multi_job_of(m.start, m.n, blockIdx.x);
+  const FpMultiJob& J = m.job[j];
+  fp_ray_tile<true, E>(J.params, J.columns, static_cast<const E*>(J.ws), nullptr, J.g, J.sched, 0,
+                       J.g.nangles, 0, J.sirt, blockIdx.x - m.start[j], out_slot);
 }
 
 }  // namespace
@@ -436,6 +463,41 @@ void launch_fp_elems(const tsgb_projector* p, const float* vol, float* sino, boo
 }
 
 }  // namespace
+
+int launch_fp_copies(const tsgb_projector* p, const float* vol, float* workspace, void* stream_) {
+  cudaStream_t stream = static_cast<cudaStream_t>(stream_);
+  // the copies only (no angles): launch_fp_elems with an empty angle range
+  if (p->tuning.fp_pair_layout)
+    launch_fp_elems(p, vol, nullptr, false, reinterpret_cast<float2*>(workspace), stream, nullptr,
+                    0, 0, false);
+  else
+    launch_fp_elems(p, vol, nullptr, false, workspace, stream, nullptr, 0, 0, false);
+  return int(cudaGetLastError());
+}
+
+bool fp_multi_eligible(const tsgb_projector* p) {
+  const long long per_pair = (long long)((p->g.rows + kFpRows - 1) / kFpRows) *
+                             ((p->g.cols + kFpCols - 1) / kFpCols);
+  return p->g.nangles <= fp_angle_chunk(p->g) &&
+         per_pair * ((p->g.nangles + 1) / 2) < (1LL << 31) / kMaxMultiJobs;
+}
+
+int launch_fp_multi(const FpMulti& m, bool pair_layout, void* stream_) {
+  cudaStream_t stream = static_cast<cudaStream_t>(stream_);
+  const long long blocks = m.start[m.n];
+  if (blocks <= 0) return int(cudaGetLastError());
+  if (pair_layout)
+    fp_ray_multi_kernel<float2><<<unsigned(blocks), dim3(kFpRows, kFpCols), 0, stream>>>(m);
+  else
+    fp_ray_multi_kernel<float><<<unsigned(blocks), dim3(kFpRows, kFpCols), 0, stream>>>(m);
+  return int(cudaGetLastError());
+}
+
+long long fp_blocks(const tsgb_projector* p) {
+  const long long per_pair = (long long)((p->g.rows + kFpRows - 1) / kFpRows) *
+                             ((p->g.cols + kFpCols - 1) / kFpCols);
+  return per_pair * fp_schedule(p, (p->g.nangles + 1) / 2).pairs;
+}
 
 int launch_fp(const tsgb_projector* p, const float* vol, float* sino, bool additive,
               float* workspace, void* stream_, const FpSirt* sirt, int angle_begin,

@@ -193,6 +193,57 @@ struct FpSirt {
   int zlayout;
 };
 
+// Multi-job launches of batched SIRT: one launch covers many small jobs, block
+// b running block b - start[j] of job j (start[j] <= b < start[j + 1]). The job
+// descriptors travel as __grid_constant__ kernel arguments.
+constexpr int kMaxMultiJobs = 48;
+
+struct FpMultiJob {
+  const AngleParams* params;
+  const ColumnEntry* columns;
+  const void* ws;  // the job's padded volume copies
+  DeviceGeometry g;
+  FpSchedule sched;
+  FpSirt sirt;
+};
+struct FpMulti {
+  int n;
+  long long start[kMaxMultiJobs + 1];
+  FpMultiJob job[kMaxMultiJobs];
+};
+
+struct BpMultiJob {
+  const AngleParams* params;
+  const ColumnEntry* columns;
+  const int* angles;  // this pass's angle ids
+  const float* pairs; // the job's residual (row-major row pairs)
+  float* vol;
+  const float* C;
+  float* scratch;     // first pass's sum (nullptr: none)
+  DeviceGeometry g;
+  int n_angles, mode; // mode: 2 = keep the sum in scratch, 3 = apply the update
+  int gx, gy;         // the job's own grid (x, y); z = blocks / (gx * gy)
+};
+struct BpMulti {
+  int n;
+  long long start[kMaxMultiJobs + 1];
+  BpMultiJob job[kMaxMultiJobs];
+};
+// kernel arguments are limited to 32764 bytes
+static_assert(sizeof(FpMulti) <= 32764 && sizeof(BpMulti) <= 32764, "multi-job tables too large");
+
+// The padded volume copies of a forward projection, no rays (fp.cu).
+int launch_fp_copies(const tsgb_projector* p, const float* vol, float* workspace, void* stream);
+// Whether a job's SIRT forward projection fits a multi-job launch (one angle
+// chunk), its block count, and the multi-job launch itself (fp.cu).
+bool fp_multi_eligible(const tsgb_projector* p);
+long long fp_blocks(const tsgb_projector* p);
+int launch_fp_multi(const FpMulti& m, bool pair_layout, void* stream);
+// Blocks of one voxel-pair backprojection pass of a job (gx, gy set), and
+// the multi-job launch of that pass over several jobs (bp.cu).
+long long bp_sep_blocks(const tsgb_projector* p, bool a_is_x, int* gx, int* gy);
+int launch_bp_sep_multi(const BpMulti& m, bool a_is_x, void* stream);
+
 // The matched backprojector of det_v-along-z angles is the z-lane kernel
 // (bp_zlane.cu, column-major weighted sinogram) unless the tuning picks the
 // voxel-pair kernel (bp.cu, row-major) or the volume's (y, x) plane is too

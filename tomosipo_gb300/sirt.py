@@ -74,6 +74,9 @@ class SirtJobState:
             nbytes = A.projector.workspace_bytes(device.index, True)
             self.ws = torch.empty(max(nbytes, 4) // 4, device=device)
 
+    def tensors(self):
+        return (self.y, self.R, self.C, self.x, self.res, self.ws)
+
     @staticmethod
     def device_bytes(A):
         """Device memory a job holds: x, C (volume) and y, R, residual (sinogram) plus workspace."""
@@ -82,6 +85,30 @@ class SirtJobState:
         sino = 4 * rows * angles * cols
         stats_ws = A.projector.stats(torch.cuda.current_device())["fp_workspace_bytes"]
         return 2 * vol + 4 * sino + 32 * angles * cols + stats_ws
+
+
+def make_states(jobs, device, n_streams=4):
+    """SirtJobState of each ``(A, y)`` or ``(A, y, x_init)``, built on up to
+    ``n_streams`` side streams at once (each job's preconditioners are one
+    forward and one backprojection, too small alone to fill the GPU); the
+    current stream waits for all of them. The results do not depend on the
+    stream a job's setup ran on."""
+    main = torch.cuda.current_stream(device)
+    if len(jobs) < 2:
+        return [SirtJobState(j[0], j[1], j[2] if len(j) > 2 else None, device) for j in jobs]
+    side = [torch.cuda.Stream(device) for _ in range(min(n_streams, len(jobs)))]
+    for s in side:
+        s.wait_stream(main)  # the inputs are written on the current stream
+    states = []
+    for i, j in enumerate(jobs):
+        with torch.cuda.stream(side[i % len(side)]):
+            st = SirtJobState(j[0], j[1], j[2] if len(j) > 2 else None, device)
+        for t in st.tensors():
+            t.record_stream(main)  # used from now on on the current stream
+        states.append(st)
+    for s in side:
+        main.wait_stream(s)
+    return states
 
 
 def autotune_jobs(operators, device):
@@ -175,8 +202,8 @@ class BatchedSirt:
         if self.device.type != "cuda":
             raise ValueError("BatchedSirt runs on CUDA tensors")
         self.tuning = autotune_jobs([j[0] for j in jobs], self.device) if autotune else {}
-        self.states = [SirtJobState(j[0], j[1], j[2] if len(j) > 2 else None, self.device)
-                       for j in jobs]
+        with torch.cuda.device(self.device):
+            self.states = make_states(jobs, self.device)
         self._native = NativeBatch(self.states)
         self._graphs = {}
 
