@@ -232,8 +232,8 @@ int tsgb_projector_get_tuning(const tsgb_projector* p, tsgb_tuning* out);
 int tsgb_projector_set_tuning(tsgb_projector* p, const tsgb_tuning* t);
 
 /* FDK backprojection (the backprojection step of tomosipo's fdk,
- * tomosipo/astra.py:374-406, which calls ASTRA's accumulate_FDK): for cone
- * beams whose detector v axis runs along z (circular and helical scans),
+ * tomosipo/astra.py:374-406, which calls ASTRA's accumulate_FDK): for any
+ * cone beam (circular, helical, rotated or tilted-detector scans),
  *   vol (+)= sum_t angle_weights[t] * q_t(u_t(x), v_t(x)) / w_t(x)^2
  * where q is the already weighted and ramp-filtered sinogram (layout as any
  * sinogram), read with bilinear interpolation and zero outside the detector,

@@ -11,7 +11,10 @@ point (pitch d = |det_u| SOD / SDD), applied as d * sum_n h[k - n] p[n]; and
 the backprojection sum_t (dbeta_t / 2) (SOD_t / U_t(x))^2 q_t(u, v) with
 bilinear detector reads (zero outside the detector). The reference point is
 the centre of voxel (nz/2, ny/2, nx/2), integer division; dbeta_t are
-central differences of the source's unwrapped angle around the z axis.
+central differences of the source's unwrapped angle around the rotation axis
+(the normalised mean of the detector's unit v vectors) through it. Short
+scans: Parker's weights (Med. Phys. 9(2), 1982) with the over-scan half-angle
+delta = (coverage - pi) / 2, times 2, on the cosine-weighted data.
 Small cases only (pure NumPy).
 """
 import math
@@ -38,18 +41,63 @@ def _normal_depths(S, D, U, V, ref, t):
     return n, np.dot(D[t] - S[t], n), np.dot(ref - S[t], n)
 
 
+def _axis_angles(S, V, ref):
+    """Rotation axis and the unwrapped source angles about it (counter-clockwise
+    about the axis, from an arbitrary in-plane direction)."""
+    axis = sum(v / np.linalg.norm(v) for v in V)
+    axis = axis / np.linalg.norm(axis)
+    # in-plane basis: Gram-Schmidt of the world axis least parallel to the axis
+    k = int(np.argmin(np.abs(axis)))
+    p = np.zeros(3)
+    p[k] = 1.0
+    p -= (p @ axis) * axis
+    p /= np.linalg.norm(p)
+    q = np.cross(axis, p)
+    ang = [math.atan2((s - ref) @ q, (s - ref) @ p) for s in S]
+    return axis, np.unwrap(ang)
+
+
 def angle_weights(vg, pg):
-    """dbeta_t / 2: half the source's angular step around the z axis through
-    the reference point (central differences of the unwrapped angle)."""
-    S, _, _, _, _, _, _, ref = _frame(vg, pg)
-    beta = np.unwrap([math.atan2(s[1] - ref[1], s[2] - ref[2]) for s in S])
+    """dbeta_t / 2: half the source's angular step around the rotation axis
+    through the reference point (central differences of the unwrapped angle)."""
+    S, _, _, V, _, _, _, ref = _frame(vg, pg)
+    _, beta = _axis_angles(S, V, ref)
     return (np.abs(np.gradient(beta)) if len(S) > 1 else np.array([2 * math.pi])) / 2
 
 
-def filtered(vg, pg, y):
+def parker(vg, pg):
+    """2 x Parker's weight of each (angle, column) of a short scan."""
+    S, D, U, V, _, _, _, ref = _frame(vg, pg)
+    axis, beta = _axis_angles(S, V, ref)
+    N = len(S)
+    C = pg.det_shape[1]
+    step = abs(beta[-1] - beta[0]) / (N - 1)
+    direction = 1.0 if beta[-1] > beta[0] else -1.0
+    delta = (abs(beta[-1] - beta[0]) + step - math.pi) / 2
+    w = np.zeros((N, C))
+    for t in range(N):
+        b = direction * (beta[t] - beta[0]) + step / 2
+        c = ref - S[t]
+        c = c - (c @ axis) * axis
+        for j in range(C):
+            d = D[t] + (j + 0.5 - C / 2) * U[t] - S[t]
+            d = d - (d @ axis) * axis
+            g = direction * math.atan2(np.cross(c, d) @ axis, c @ d)
+            assert abs(g) <= delta, "scan shorter than pi plus the fan angle"
+            if b < 2 * (delta - g):
+                w[t, j] = math.sin(math.pi / 4 * b / (delta - g)) ** 2
+            elif b <= math.pi - 2 * g:
+                w[t, j] = 1.0
+            elif b <= math.pi + 2 * delta:
+                w[t, j] = math.sin(math.pi / 4 * (math.pi + 2 * delta - b) / (delta + g)) ** 2
+    return 2 * w
+
+
+def filtered(vg, pg, y, short_scan=False):
     """Cosine-weighted, ramp-filtered sinogram (fp64, (rows, angles, cols)): steps
     1 and 2 of FDK, with the Ram-Lak filter as a direct convolution."""
     S, D, U, V, _, _, _, ref = _frame(vg, pg)
+    pw = parker(vg, pg) if short_scan else None
     y = np.asarray(y, dtype=np.float64)
     R, N, C = y.shape
     k = np.arange(-(C - 1), C)
@@ -65,11 +113,13 @@ def filtered(vg, pg, y):
         d = np.linalg.norm(U[t]) * sod / sdd
         X = D[t] + a[:, None, None] * V[t] + b[None, :, None] * U[t]
         p = y[:, t, :] * sdd / np.linalg.norm(X - S[t], axis=-1)
+        if pw is not None:
+            p = p * pw[t][None, :]
         q[:, t, :] = np.stack([np.convolve(p[r], h1)[C - 1:2 * C - 1] for r in range(R)]) / d
     return q
 
 
-def fdk(vg, pg, y):
+def fdk(vg, pg, y, short_scan=False):
     """FDK reconstruction (fp64 volume) of sinogram ``y`` ((rows, angles, cols))."""
     S, D, U, V, shape, vs, llc, ref = _frame(vg, pg)
     R, N, C = np.shape(y)
@@ -78,7 +128,7 @@ def fdk(vg, pg, y):
     P = np.stack(np.meshgrid(*grids, indexing="ij"), axis=-1).reshape(-1, 3)
     out = np.zeros(P.shape[0])
     half_dbeta = angle_weights(vg, pg)
-    Q = filtered(vg, pg, y)
+    Q = filtered(vg, pg, y, short_scan)
     for t in range(N):
         n, sdd, sod = _normal_depths(S, D, U, V, ref, t)
         q = Q[:, t, :]

@@ -11,21 +11,71 @@ from tests.helpers import rel_l2
 from tomosipo_gb300 import fdk
 
 
+# a scan of pi + 0.5 rad: the detector's fan half-angle is about 0.17 rad
+SHORT = np.linspace(0, np.pi + 0.5, 17, endpoint=False)
+
+
 def _scans():
-    circular = ts.cone(angles=17, shape=(9, 13), size=(1.2, 1.6), src_orig_dist=3,
-                       src_det_dist=4.5)
+    kw = dict(shape=(9, 13), size=(1.2, 1.6), src_orig_dist=3, src_det_dist=4.5)
+    circular = ts.cone(angles=17, **kw)
     lift = np.stack([np.linspace(-0.2, 0.2, 17), np.zeros(17), np.zeros(17)], axis=1)
-    return {"circular": circular, "helical": ts.translate(lift) * circular.to_vec()}
+    rot = ts.rotate(pos=0, axis=(1.0, 0.4, -0.3), angles=0.5)
+    return {"circular": circular, "helical": ts.translate(lift) * circular.to_vec(),
+            "rotated": rot * circular.to_vec(), "short": ts.cone(angles=SHORT, **kw),
+            "short_rotated_reversed": rot * ts.cone(angles=-SHORT, **kw).to_vec()}
 
 
-@pytest.mark.parametrize("scan", ["circular", "helical"])
+@pytest.mark.parametrize("scan", ["circular", "helical", "rotated", "short",
+                                  "short_rotated_reversed"])
 def test_filter_and_angle_weights_match_the_oracle(scan):
     pg = _scans()[scan]
+    short = scan.startswith("short")
     vg = ts.volume(shape=(10, 12, 14), size=(0.8, 1, 1.1), pos=(0.05, -0.1, 0.02))
     y = np.random.default_rng(1).random((9, 17, 13)).astype(np.float32)
-    q = fdk.fdk_filter(vg, pg, torch.from_numpy(y)).double().numpy()
-    assert rel_l2(q, fdk_oracle.filtered(vg, pg, y.astype(np.float64))) < 1e-5  # measured 1.2e-7
+    q = fdk.fdk_filter(vg, pg, torch.from_numpy(y), short_scan=short).double().numpy()
+    ref = fdk_oracle.filtered(vg, pg, y.astype(np.float64), short_scan=short)
+    assert rel_l2(q, ref) < 1e-5  # measured 1.2e-7
     assert np.abs(fdk.fdk_constants(vg, pg)[2] - fdk_oracle.angle_weights(vg, pg)).max() < 1e-12
+    if short:
+        assert np.abs(fdk.short_scan_weights(vg, pg) - fdk_oracle.parker(vg, pg)).max() < 1e-12
+
+
+def test_rotation_axis_of_a_rotated_scan_is_the_rotated_z_axis():
+    rot = ts.rotate(pos=0, axis=(1.0, 0.4, -0.3), angles=0.5)
+    pg = _scans()["rotated"]
+    V = np.asarray(pg.det_v, dtype=np.float64)
+    axis, e1, e2 = fdk.rotation_frame(V)
+    z = np.asarray(rot.transform_vec(np.array([[1.0, 0, 0]])), dtype=np.float64).reshape(3)
+    assert abs(abs(axis @ (z / np.linalg.norm(z))) - 1) < 1e-12
+    assert abs(e1 @ axis) < 1e-12 and abs(e2 @ axis) < 1e-12 and abs(e1 @ e2) < 1e-12
+    # full-circle angle steps about the rotated axis through the origin (the
+    # anchor of an odd-sided volume centred there) are 2 pi / 17, as about z
+    w = fdk.fdk_constants(ts.volume(shape=9, size=1), pg)[2]
+    assert np.abs(w - np.pi / 17).max() < 1e-12
+
+
+def test_parker_weights_of_each_redundant_pair_sum_to_one():
+    delta = 0.3
+    rng = np.random.default_rng(2)
+    gamma = rng.uniform(-delta, delta, 200)
+    beta = rng.uniform(0, np.pi + 2 * delta, 200)
+    conj = beta + np.pi + 2 * gamma  # the same line, measured later ...
+    early = conj <= np.pi + 2 * delta
+    beta_e, gamma_e = beta[early], gamma[early]
+    s = fdk.parker_weights(beta_e, gamma_e, delta) + fdk.parker_weights(
+        beta_e + np.pi + 2 * gamma_e, -gamma_e, delta)
+    assert np.abs(s - 1).max() < 1e-12
+    # ... and lines measured once have weight 1
+    once = (beta >= 2 * (delta - gamma)) & (beta <= np.pi - 2 * gamma)
+    assert np.all(fdk.parker_weights(beta[once], gamma[once], delta) == 1)
+    assert np.all(fdk.parker_weights(np.array([-0.1, np.pi + 2 * delta + 0.1]), 0.0, delta) == 0)
+
+
+def test_short_scan_needs_pi_plus_the_fan_angle():
+    pg = ts.cone(angles=np.linspace(0, np.pi + 0.2, 17, endpoint=False), shape=(9, 13),
+                 size=(1.2, 1.6), src_orig_dist=3, src_det_dist=4.5)
+    with pytest.raises(ValueError, match="pi plus the fan angle"):
+        fdk.short_scan_weights(ts.volume(shape=8), pg)
 
 
 def test_ramp_spectrum_is_the_zero_padded_ram_lak_kernel():

@@ -76,14 +76,16 @@ def backward(*data, voxel_supersampling=1, detector_supersampling=1, additive=Fa
             projector=projector, backprojector=backprojector)
 
 
-def fdk(vol_data, proj_data, *, voxel_supersampling=1, detector_supersampling=1):
+def fdk(vol_data, proj_data, *, voxel_supersampling=1, detector_supersampling=1,
+        short_scan=False):
     """FDK reconstruction of ``proj_data`` added into ``vol_data``.
 
     As the reference's ``accumulate_FDK`` call, the reconstruction is added
-    to the volume's current values. Cone beams whose detector v axis runs
-    along z only (``tomosipo_gb300.fdk``). Supersampling factors are accepted
-    for signature compatibility; FDK's backprojection reads the detector once
-    per voxel.
+    to the volume's current values. Any cone-beam geometry
+    (``tomosipo_gb300.fdk``); ``short_scan`` adds Parker's redundancy weights
+    (not in the reference's call). Supersampling factors are accepted for
+    signature compatibility; FDK's backprojection reads the detector once per
+    voxel.
     """
     from .fdk import fdk_constants, fdk_reconstruct
     from .projector import _as_device_tensor, _cuda_device_for_host_data
@@ -93,7 +95,8 @@ def fdk(vol_data, proj_data, *, voxel_supersampling=1, detector_supersampling=1)
     dev = vol.device if isinstance(vol, torch.Tensor) and vol.is_cuda else _cuda_device_for_host_data()
     y, _ = _as_device_tensor(sino, dev, copy_in=True)
     x, copy_back = _as_device_tensor(vol, dev, copy_in=True)
-    fdk_reconstruct(vol_data.geometry, proj_data.geometry, y, out=x, additive=True)
+    fdk_reconstruct(vol_data.geometry, proj_data.geometry, y, out=x, additive=True,
+                    short_scan=short_scan)
     if copy_back:
         import numpy as np
 

@@ -433,10 +433,14 @@ __device__ __forceinline__ float detector_bilinear(const float* __restrict__ bas
   return fmaf(fv, bot - top, top);
 }
 
+// Voxel-driven bilinear backprojection of any angle (voxel supersampling
+// included). With angle_w (cone beams) the weight is FDK's angle_w[theta] / w^2
+// (w = pw . [P, 1], the voxel's depth along the detector normal relative to
+// the anchor's) instead of the bilinear backprojector's.
 __global__ void __launch_bounds__(kBpX* kBpY)
     bp_bilinear_kernel(const AngleParams* __restrict__ params, const int* __restrict__ angles,
                        int n_angles, const float* __restrict__ sino, float* __restrict__ vol,
-                       DeviceGeometry g, int additive) {
+                       DeviceGeometry g, int additive, const float* __restrict__ angle_w) {
   const int x = blockIdx.x * kBpX + threadIdx.x;
   const int y = blockIdx.y * kBpY + threadIdx.y;
   const int z0 = blockIdx.z * kRunZBil;
@@ -466,7 +470,9 @@ __global__ void __launch_bounds__(kBpX* kBpY)
             const float nw = fmaf(ap.pw[0], zt, fmaf(ap.pw[1], yt, fmaf(ap.pw[2], xt, ap.pw[3])));
             const float inw = 1.0f / nw;
             float c = ap.bil_scale;
-            if (cone) {
+            if (angle_w) {
+              c = nw > 0.0f ? __ldg(angle_w + theta) * inw * inw : 0.0f;
+            } else if (cone) {
               const float dz = (zt - ap.src[0]) * g.vs[0], dy = (yt - ap.src[1]) * g.vs[1];
               const float dx = (xt - ap.src[2]) * g.vs[2];
               const float len = sqrtf(fmaf(dz, dz, fmaf(dy, dy, dx * dx)));
@@ -935,7 +941,7 @@ int launch_bp_bilinear(const tsgb_projector* p, float* vol, const float* sino, b
     const dim3 grid((g.nx + kBpX - 1) / kBpX, (g.ny + kBpY - 1) / kBpY,
                     (g.nz + kRunZBil - 1) / kRunZBil);
     bp_bilinear_kernel<<<grid, block, 0, stream>>>(p->d_params, p->d_bil_slow, p->n_bil_slow, sino,
-                                                   vol, g, (additive || written) ? 1 : 0);
+                                                   vol, g, (additive || written) ? 1 : 0, nullptr);
   }
   return int(cudaGetLastError());
 }
@@ -944,12 +950,24 @@ int launch_bp_fdk(const tsgb_projector* p, float* vol, const float* sino, const 
                   bool additive, float* workspace, void* stream_) {
   cudaStream_t stream = static_cast<cudaStream_t>(stream_);
   const DeviceGeometry& g = p->g;
-  const long long total = (long long)(g.rows + 2 * kRowPad) * g.nangles * (g.cols + 2 * kColPad);
-  const long long blocks = (total + 255) / 256;
-  float4* quads = reinterpret_cast<float4*>(workspace);
-  bp_bilinear_prep_kernel<<<int(blocks < 152LL * 64 ? blocks : 152LL * 64), 256, 0, stream>>>(
-      sino, quads, g);
-  launch_bil_z<kBilFdk>(p, quads, vol, additive, angle_w, stream);
+  bool written = false;
+  if (p->n_bil_fast > 0) {
+    const long long total = (long long)(g.rows + 2 * kRowPad) * g.nangles * (g.cols + 2 * kColPad);
+    const long long blocks = (total + 255) / 256;
+    float4* quads = reinterpret_cast<float4*>(workspace);
+    bp_bilinear_prep_kernel<<<int(blocks < 152LL * 64 ? blocks : 152LL * 64), 256, 0, stream>>>(
+        sino, quads, g);
+    launch_bil_z<kBilFdk>(p, quads, vol, additive, angle_w, stream);
+    written = true;
+  }
+  if (p->n_bil_slow > 0 || !written) {
+    // angles whose projection depends on z (tilted detectors, rotated scans)
+    const dim3 grid((g.nx + kBpX - 1) / kBpX, (g.ny + kBpY - 1) / kBpY,
+                    (g.nz + kRunZBil - 1) / kRunZBil);
+    bp_bilinear_kernel<<<grid, dim3(kBpX, kBpY), 0, stream>>>(
+        p->d_params, p->d_bil_slow, p->n_bil_slow, sino, vol, g, (additive || written) ? 1 : 0,
+        angle_w);
+  }
   return int(cudaGetLastError());
 }
 

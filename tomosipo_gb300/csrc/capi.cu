@@ -345,10 +345,7 @@ int tsgb_fdk_backproject(tsgb_projector* p, float* vol, const float* filtered, c
   g_last_error.clear();
   if (!p || !vol || !filtered || !angle_weights)
     return fail(TSGB_ERR_INVALID, "NULL projector or data pointer");
-  if (p->g.kind != TSGB_CONE || p->n_bil_slow > 0 || p->n_bil_fast == 0)
-    return fail(TSGB_ERR_INVALID,
-                "FDK needs a cone beam whose detector v axis runs along z (circular or helical "
-                "scans)");
+  if (p->g.kind != TSGB_CONE) return fail(TSGB_ERR_INVALID, "FDK needs a cone beam");
   const int64_t need = tsgb_bp_workspace_bytes(p, TSGB_BP_BILINEAR);
   if (!workspace || workspace_bytes < need)
     return fail(TSGB_ERR_WORKSPACE, "FDK needs " + std::to_string(need) + " bytes of workspace");

@@ -16,13 +16,18 @@ Feldkamp-Davis-Kress method for flat detectors (J. Opt. Soc. Am. A 1(6),
    (U_t(x) the voxel's depth along the normal) with bilinear detector reads:
    ``tsgb_fdk_backproject``.
 
-dbeta_t is the source's angular step around the z axis through the volume
-anchor (central differences of the unwrapped angles). A full circle (2 pi)
-is the FDK case; shorter scans would need redundancy (Parker) weights, which
-are not applied, and helical scans are approximations as in any FDK.
-Steps 1 and 2 are torch element-wise ops and a batched FFT on the device.
-Cone beams whose detector v axis runs along z are supported (circular and
-helical ``cone``/``cone_vec``); other geometries raise ``ValueError``.
+dbeta_t is the source's angular step around the rotation axis through the
+volume anchor (central differences of the unwrapped angles); the axis is the
+mean direction of the detector's v axis, which FDK's setup keeps parallel to
+it (z for ``ts.cone``). A full circle (2 pi) is the FDK case, and helical
+scans are approximations as in any FDK. Short scans (``short_scan=True``:
+pi plus the fan angle, up to a full circle) get Parker's redundancy weights
+(D. L. Parker, Med. Phys. 9(2), 1982) before filtering, generalised to the
+scan's own over-scan angle; the reference's ``accumulate_FDK`` call applies
+none, so they are off by default. Steps 1 and 2 are torch element-wise ops
+and a batched FFT on the device. Any cone geometry is accepted: angles whose
+projection does not depend on z take the z-flat bilinear kernel, the others
+(tilted detectors, rotated scans) the general bilinear kernel.
 """
 import math
 
@@ -30,6 +35,38 @@ import numpy as np
 import torch
 
 from . import _native
+
+
+def _vectors(pg):
+    v = pg.to_vec()
+    return tuple(np.asarray(a, dtype=np.float64) for a in (v.src_pos, v.det_pos, v.det_u, v.det_v))
+
+
+def _anchor(vg):
+    shape = np.array(vg.shape)
+    return np.asarray(vg.lower_left_corner)[0] + (shape // 2 + 0.5) * np.asarray(vg.voxel_sizes)[0]
+
+
+def rotation_frame(V):
+    """Unit rotation axis (the mean direction of the detector v vectors) and
+    two unit vectors e1, e2 spanning the plane normal to it, with
+    e2 = axis x e1 (so angles atan2(r.e2, r.e1) grow counter-clockwise about
+    the axis). For an axis along z, e1 is x."""
+    axis = (V / np.linalg.norm(V, axis=1, keepdims=True)).mean(axis=0)
+    axis /= np.linalg.norm(axis)
+    # the coordinate axis least aligned with the rotation axis, orthogonalised
+    e1 = np.eye(3)[[2, 1, 0][int(np.argmin(np.abs(axis[[2, 1, 0]])))]]
+    e1 = e1 - np.dot(e1, axis) * axis
+    e1 /= np.linalg.norm(e1)
+    return axis, e1, np.cross(axis, e1)
+
+
+def source_angles(S, anchor, V):
+    """Unwrapped angle of each source position about the rotation axis through
+    ``anchor``."""
+    _, e1, e2 = rotation_frame(V)
+    r = S - anchor[None]
+    return np.unwrap(np.arctan2(r @ e2, r @ e1))
 
 
 def fdk_constants(vg, pg):
@@ -42,10 +79,8 @@ def fdk_constants(vg, pg):
     """
     if not getattr(pg, "is_cone", False):
         raise ValueError("FDK reconstructs cone-beam geometries only")
-    v = pg.to_vec()
-    S, D, U, V = (np.asarray(a, dtype=np.float64) for a in (v.src_pos, v.det_pos, v.det_u, v.det_v))
-    shape = np.array(vg.shape)
-    anchor = np.asarray(vg.lower_left_corner)[0] + (shape // 2 + 0.5) * np.asarray(vg.voxel_sizes)[0]
+    S, D, U, V = _vectors(pg)
+    anchor = _anchor(vg)
     n = np.cross(U, V)
     n /= np.linalg.norm(n, axis=1, keepdims=True)
     n *= np.sign(np.einsum("ij,ij->i", D - S, n))[:, None]
@@ -54,9 +89,64 @@ def fdk_constants(vg, pg):
     if np.any(sdd <= 0) or np.any(sod <= 0):
         raise ValueError("FDK needs the volume and the detector in front of the source")
     pitch = np.linalg.norm(U, axis=1) * sod / sdd
-    beta = np.unwrap(np.arctan2(S[:, 1] - anchor[1], S[:, 2] - anchor[2]))
+    beta = source_angles(S, anchor, V)
     dbeta = np.abs(np.gradient(beta)) if len(beta) > 1 else np.array([2 * math.pi])
     return sdd, pitch, dbeta / 2
+
+
+def parker_weights(beta, gamma, delta):
+    """Parker's redundancy weights for a short scan over [0, pi + 2 delta].
+
+    ``beta``: source angle from the scan's start, in its direction of
+    rotation; ``gamma``: fan angle of the ray, positive in the same direction
+    (so the ray (beta, gamma) is measured again at (beta + pi + 2 gamma,
+    -gamma)); ``delta`` >= max |gamma|: half the over-scan. The two weights of
+    every such pair sum to 1. Arrays broadcast.
+    """
+    beta, gamma = np.asarray(beta, dtype=np.float64), np.asarray(gamma, dtype=np.float64)
+    lo = 2 * (delta - gamma)  # end of the ramp-up
+    hi = math.pi - 2 * gamma  # start of the ramp-down
+    with np.errstate(divide="ignore", invalid="ignore"):
+        up = np.sin(math.pi / 4 * beta / (delta - gamma)) ** 2
+        down = np.sin(math.pi / 4 * (math.pi + 2 * delta - beta) / (delta + gamma)) ** 2
+    w = np.where(beta < lo, up, np.where(beta <= hi, 1.0, down))
+    return np.where((beta < 0) | (beta > math.pi + 2 * delta), 0.0, w)
+
+
+def short_scan_weights(vg, pg):
+    """Twice Parker's weights of every (angle, detector column), (angles, cols)
+    fp64: a short scan measures each line once where a full circle measures it
+    twice, and FDK's angle weight dbeta / 2 assumes the latter.
+
+    The scan covers Delta = |beta_last - beta_first| + mean |dbeta|, centred
+    on the source angles; delta = (Delta - pi) / 2 must cover the largest fan
+    angle of the detector's columns (measured in the plane normal to the
+    rotation axis)."""
+    S, D, U, V = _vectors(pg)
+    anchor = _anchor(vg)
+    axis, _, _ = rotation_frame(V)
+    beta = source_angles(S, anchor, V)
+    n = len(beta)
+    step = abs(beta[-1] - beta[0]) / (n - 1) if n > 1 else 2 * math.pi
+    sign = 1.0 if n < 2 or beta[-1] >= beta[0] else -1.0
+    coverage = abs(beta[-1] - beta[0]) + step
+    delta = (coverage - math.pi) / 2
+    cols = pg.det_shape[1]
+    b = np.arange(cols) + 0.5 - cols / 2
+
+    def perp(w):
+        return w - (w @ axis)[..., None] * axis
+
+    c = perp(anchor[None] - S)  # central ray (angles, 3)
+    d = perp(D[:, None, :] + b[None, :, None] * U[:, None, :] - S[:, None, :])  # (angles, cols, 3)
+    cross = np.cross(c[:, None, :], d) @ axis
+    gamma = sign * np.arctan2(cross, np.einsum("ij,ikj->ik", c, d))
+    if not delta >= np.abs(gamma).max():
+        raise ValueError(
+            "a short scan must cover pi plus the fan angle: {:.4f} rad covered, {:.4f} needed"
+            .format(coverage, math.pi + 2 * np.abs(gamma).max()))
+    rel = sign * (beta - beta[0]) + step / 2
+    return 2 * parker_weights(rel[:, None], gamma, delta)
 
 
 def ramp_spectrum(cols, device):
@@ -70,13 +160,15 @@ def ramp_spectrum(cols, device):
     return torch.from_numpy(np.fft.rfft(g).real.astype(np.float32)).to(device), length
 
 
-def fdk_filter(vg, pg, y, angle_chunk=64):
-    """Cosine-weighted, ramp-filtered copy of sinogram ``y`` (a CUDA tensor)."""
+def fdk_filter(vg, pg, y, angle_chunk=64, short_scan=False):
+    """Cosine-weighted (and with ``short_scan`` Parker-weighted), ramp-filtered
+    copy of sinogram ``y`` (a CUDA tensor)."""
     rows, nang, cols = y.shape
     dev = y.device
     sdd, pitch, _ = fdk_constants(vg, pg)
-    v = pg.to_vec()
-    S, D, U, V = (np.asarray(a, dtype=np.float64) for a in (v.src_pos, v.det_pos, v.det_u, v.det_v))
+    S, D, U, V = _vectors(pg)
+    parker = (torch.from_numpy(short_scan_weights(vg, pg).astype(np.float32)).to(dev)
+              if short_scan else None)
     w0 = D - S
     # |X - S|^2 = |w0 + a V + b U|^2 with a, b the pixel offsets from the centre
     per_angle = np.stack([
@@ -97,6 +189,8 @@ def fdk_filter(vg, pg, y, angle_chunk=64):
                  + A * k[None, :, 3, None] + B * k[None, :, 4, None] + A * B * k[None, :, 5, None])
         cosw = (k[None, :, 6, None] / torch.sqrt(dist2)).to(torch.float32)
         p = y[:, t0:t1, :].to(torch.float32) * cosw
+        if parker is not None:
+            p = p * parker[None, t0:t1, :]
         f = torch.fft.irfft(torch.fft.rfft(p, n=length, dim=-1) * spec, n=length, dim=-1)[..., :cols]
         q[:, t0:t1, :] = f * k[None, :, 7, None].to(torch.float32)
     return q
@@ -117,18 +211,19 @@ def fdk_backproject(projector, vol, q, angle_weight, additive):
                       "tsgb_fdk_backproject")
 
 
-def fdk_reconstruct(vg, pg, y, out=None, additive=False, projector=None):
+def fdk_reconstruct(vg, pg, y, out=None, additive=False, projector=None, short_scan=False):
     """FDK reconstruction of sinogram ``y`` (CUDA tensor, (rows, angles, cols)).
 
     Returns ``out`` (a CUDA volume tensor, created if None; added to when
-    ``additive``).
+    ``additive``). ``short_scan``: apply Parker's redundancy weights (scans of
+    pi plus the fan angle or more, less than a full circle).
     """
     from .projector import create_projector
 
     if not (isinstance(y, torch.Tensor) and y.is_cuda):
         raise ValueError("fdk_reconstruct expects a CUDA tensor sinogram")
     projector = projector or create_projector(vg, pg)
-    q = fdk_filter(vg, pg, y)
+    q = fdk_filter(vg, pg, y, short_scan=short_scan)
     if out is None:
         out = torch.zeros(tuple(vg.shape), dtype=torch.float32, device=y.device)
         additive = True
