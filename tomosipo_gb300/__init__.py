@@ -32,6 +32,7 @@ from . import links
 from . import phantom
 from . import types
 from . import vector_calc
+from .hostmem import host_buffer
 
 # Used for floating-point equality checks and the SIRT clipping 1 / epsilon
 # (tomosipo/__init__.py:41).
