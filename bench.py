@@ -388,6 +388,21 @@ def bench_general_bp(torch, ts, device, steps, n=256, angles=360, det=(256, 384)
     torch.cuda.synchronize()
     fp = statistics.mean(e[0].elapsed_time(e[1]) for e in ev)
     bp = statistics.mean(e[1].elapsed_time(e[2]) for e in ev)
+    # the same backprojection with one thread per voxel (tuning bp_general = 1)
+    kernel = A.projector.get_tuning(device.index)["bp_general"]
+    A.projector.set_tuning(device.index, bp_general=1)
+    v1 = torch.empty_like(v)
+    A.T(y, out=v1)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(steps):
+        A.T(y, out=v1)
+    e1.record()
+    torch.cuda.synchronize()
+    bp_voxel = e0.elapsed_time(e1) / steps
+    A.projector.set_tuning(device.index, bp_general=kernel)
+    same = bool(torch.equal(v, v1))
     U = n ** 3 * angles
     peak, _ = measured_peak_hbm()
     return {"config": f"cone {n}^3, {angles} angles, detector {det[0]}x{det[1]}, tilted 0.4 rad "
@@ -395,7 +410,11 @@ def bench_general_bp(torch, ts, device, steps, n=256, angles=360, det=(256, 384)
                       "general backprojector",
             "fp_ms": fp, "general_bp_ms": bp,
             "bp_gups": U / (bp / 1e3) / 1e9, "fp_gups": U / (fp / 1e3) / 1e9,
-            "bp_roofline_frac": BYTES_PER_UPDATE * U / (bp / 1e3) / 1e9 / peak}
+            "bp_roofline_frac": BYTES_PER_UPDATE * U / (bp / 1e3) / 1e9 / peak,
+            "bp_kernel": "voxel boxes staging each angle's detector region (bp_general 0)"
+                         if kernel == 0 else "one thread per voxel (bp_general 1)",
+            "per_voxel_kernel_bp_ms": bp_voxel,
+            "per_voxel_kernel_equal": same}
 
 
 def helical_cone_vec(ts, n, angles, rows, cols, rng, jitter_voxels=0.5):
@@ -535,6 +554,27 @@ def bench_lpd(torch, ts, device, batch=8, n=128, angles=128, iterations=10, chan
     # projector work per step: forward 2 x (FP + BP) per iteration (recomputed),
     # backward one BP and one FP per iteration, each over the batch
     updates = iterations * 3 * 2 * batch * n ** 3 * angles
+    # The projector's own time: the batched FP and BP calls the network makes
+    # (one call over the batch each), timed alone on the same operator and shapes.
+    xb = x.detach().reshape(batch, n, n, n).contiguous()
+    yb = torch.empty((batch, *A.range_shape), device=device)
+    vb = torch.empty_like(xb)
+    A._apply_batch(xb, yb)
+    A.T._apply_batch(yb, vb)
+    torch.cuda.synchronize()
+    pe = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
+    reps = 5
+    pe[0].record()
+    for _ in range(reps):
+        A._apply_batch(xb, yb)
+    pe[1].record()
+    for _ in range(reps):
+        A.T._apply_batch(yb, vb)
+    pe[2].record()
+    torch.cuda.synchronize()
+    fp_call_ms = pe[0].elapsed_time(pe[1]) / reps
+    bp_call_ms = pe[1].elapsed_time(pe[2]) / reps
+    proj_ms = iterations * 3 * (fp_call_ms + bp_call_ms)
     return {
         "config": f"batch {batch}, cone {n}^3, {angles} angles, detector {n}x{3 * n // 2}, "
                   f"{iterations} unrolled iterations, 3-layer 3D CNN with {channels} channels, "
@@ -542,6 +582,15 @@ def bench_lpd(torch, ts, device, batch=8, n=128, angles=128, iterations=10, chan
         "ms_per_step": ms,
         "samples_per_s": batch * 1e3 / ms,
         "projector_gups_in_step": updates / (ms / 1e3) / 1e9,
+        "projector_gups_in_step_note": "projector updates per step / whole training step time "
+                                       "(convolutions included)",
+        "projector_fp_batch_ms": fp_call_ms,
+        "projector_bp_batch_ms": bp_call_ms,
+        "projector_ms_per_step": proj_ms,
+        "projector_share_of_step": proj_ms / ms,
+        "projector_gups": updates / (proj_ms / 1e3) / 1e9,
+        "projector_note": f"one batched FP and one batched BP call over the {batch} slices, timed "
+                          f"alone ({reps} calls each); {3 * iterations} of each per step",
         "peak_mem_gb": torch.cuda.max_memory_allocated(device) / 1e9,
         "loss": float(loss.detach()),
     }
@@ -650,14 +699,17 @@ def run_ours(args, rank, world, local_rank):
     ms_per_step = total_ms / args.steps
     value = whole_job_gups(world, 2 * U, args.steps, total_ms / 1e3)
 
-    # End to end through the public API with pinned host buffers: every step
-    # copies the volume in, projects, copies the sinogram out, copies it back
-    # in, backprojects and copies the volume out (A(x_host), A.T(y_host)).
+    # End to end through the public API with page-locked host buffers
+    # (ts.host_buffer: huge-page backed, so DMA keeps its rate on a host that
+    # other processes have used): every step copies the volume in, projects,
+    # copies the sinogram out, copies it back in, backprojects and copies the
+    # volume out (A(x_host), A.T(y_host)).
     e2e = None
     if not args.no_e2e:
-        xh = x.cpu().pin_memory()
-        yh = torch.empty(A.range_shape, dtype=torch.float32).pin_memory()
-        vh = torch.empty(A.domain_shape, dtype=torch.float32).pin_memory()
+        xh = ts.host_buffer(A.domain_shape)
+        xh.copy_(x.cpu())
+        yh = ts.host_buffer(A.range_shape)
+        vh = ts.host_buffer(A.domain_shape)
         for _ in range(max(1, args.warmup)):
             A(xh, out=yh)
             A.T(yh, out=vh)
@@ -695,7 +747,7 @@ def run_ours(args, rank, world, local_rank):
             "fp_ms": 1e3 * statistics.median(c[0] for c in calls),
             "bp_ms": 1e3 * statistics.median(c[1] for c in calls),
             "per_step_device_ms": breakdown,
-            "path": "ts.operator A(x_host)->y_host, A.T(y_host)->x_host, pinned buffers",
+            "path": "ts.operator A(x_host)->y_host, A.T(y_host)->x_host, page-locked huge-page host buffers (ts.host_buffer)",
         }
 
     if rank != 0:
