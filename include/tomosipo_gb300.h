@@ -208,7 +208,7 @@ int tsgb_sirt_batch_destroy(tsgb_sirt_batch* b);
  * cross is read from HBM once and reused from L2 across the group's angles.
  * Any values >= 1 give bit-identical results. bp_kernel and bp_shape pick the
  * matched backprojector and its warp shape; they change only the order of
- * fp32 sums. Defaults are set at creation; the Python autotuner times
+ * fp32 sums. bp_general picks the kernel of angles outside that backprojector. Defaults are set at creation; the Python autotuner times
  * candidates and sets the fastest. Used by tsgb_direct_fp / tsgb_direct_bp and
  * by the batched SIRT passes. No counterpart in the reference (ASTRA's launch
  * shapes are fixed). */
@@ -225,7 +225,11 @@ typedef struct {
                              voxels along z per lane x warps per block):
                              0: 4x8x4, 1: 4x8x8, 2: 4x16x8, 3: 4x16x16,
                              4: 3x16x8, 5: 4x4x4, 6: 4x2x4 */
-  int32_t reserved[2];    /* must be 0 */
+  int32_t bp_general;     /* matched backprojection of the other angles (tilted
+                             detectors): 0: blocks over voxel boxes that stage
+                             each angle's detector region in shared memory,
+                             1: one thread per voxel; both give the same sums */
+  int32_t reserved;       /* must be 0 */
 } tsgb_tuning;
 
 int tsgb_projector_get_tuning(const tsgb_projector* p, tsgb_tuning* out);

@@ -69,11 +69,12 @@ def test_set_tuning_rejects_bad_values(dev):
     h = A.projector.handle(dev.index)
     lib = _native.load()
     for bad in (dict(fp_patch_rows=0), dict(fp_patch_cols=-1), dict(fp_group_pairs=0),
-                dict(fp_pair_layout=2), dict(bp_kernel=2), dict(bp_shape=-1), dict(bp_shape=7)):
+                dict(fp_pair_layout=2), dict(bp_kernel=2), dict(bp_shape=-1), dict(bp_shape=7),
+                dict(bp_general=2), dict(bp_general=-1)):
         t = _native.Tuning(**dict(dict(fp_patch_rows=1, fp_patch_cols=1, fp_group_pairs=1), **bad))
         assert lib.tsgb_projector_set_tuning(h, ctypes.byref(t)) == -1
     t = _native.Tuning(fp_patch_rows=1, fp_patch_cols=1, fp_group_pairs=1)
-    t.reserved[1] = 1
+    t.reserved = 1
     assert lib.tsgb_projector_set_tuning(h, ctypes.byref(t)) == -1
     with pytest.raises(ValueError):
         A.projector.set_tuning(dev.index, tile=3)

@@ -54,7 +54,8 @@ class Tuning(ctypes.Structure):
         ("fp_pair_layout", ctypes.c_int32),
         ("bp_kernel", ctypes.c_int32),
         ("bp_shape", ctypes.c_int32),
-        ("reserved", ctypes.c_int32 * 2),
+        ("bp_general", ctypes.c_int32),
+        ("reserved", ctypes.c_int32),
     ]
 
 

@@ -339,7 +339,80 @@ __device__ __forceinline__ float coord(int axis, float z, float y, float x) {
   return axis == 0 ? z : (axis == 1 ? y : x);
 }
 
-// One thread per voxel; any geometry.
+// Where the weighted value W y of pixel (iv, iu) at angle theta sits in a
+// row-pair sinogram: the first half of pair base + iv * s_row + iu * s_col,
+// row-major (rows nangles * cols apart) or column-major (rows adjacent).
+struct PairView {
+  size_t s_row, s_col;
+  __device__ __forceinline__ PairView(const DeviceGeometry& g, int zlayout)
+      : s_row(zlayout ? 1 : (size_t)g.nangles * g.cols),
+        s_col(zlayout ? size_t(g.rows + 2 * kRowPad) : 1) {}
+  __device__ __forceinline__ const float2* base(const float2* sinow, const DeviceGeometry& g,
+                                                int theta, int zlayout) const {
+    return zlayout ? sinow + (size_t)theta * g.cols * s_col + kRowPad
+                   : sinow + ((size_t)kRowPad * g.nangles + theta) * g.cols;
+  }
+};
+
+// The ray of pixel (iu, iv) at one angle, as the forward projector computes it.
+__device__ __forceinline__ Ray pixel_ray(const AngleParams& ap,
+                                         const ColumnEntry* __restrict__ columns,
+                                         const DeviceGeometry& g, int theta, int iu, int iv) {
+  const float vt = float(iv - g.ov);
+  return ap.separable ? ray_column(columns[(size_t)theta * g.cols + iu], vt)
+                      : ray_general(ap, float(iu - g.ou), vt);
+}
+
+// Matched-backprojection terms of one voxel (anchored zt, yt, xt) for one
+// angle of any geometry, added to acc: project the four corners
+// (kt, it -+ 1, jt -+ 1) of the voxel's tent footprint on its plane of the
+// dominant axis, and test every pixel of their bounding box with the forward
+// projector's ray formula. Rows outer, columns inner.
+__device__ __forceinline__ float general_voxel_terms(const AngleParams& ap,
+                                                     const ColumnEntry* __restrict__ columns,
+                                                     const float2* __restrict__ base,
+                                                     const PairView& pv, const DeviceGeometry& g,
+                                                     int theta, float zt, float yt, float xt,
+                                                     float acc) {
+  const float kt = coord(ap.d, zt, yt, xt);
+  const float it = coord(ap.a, zt, yt, xt);
+  const float jt = coord(ap.b, zt, yt, xt);
+  const float nu = fmaf(ap.pu[0], zt, fmaf(ap.pu[1], yt, fmaf(ap.pu[2], xt, ap.pu[3])));
+  const float nv = fmaf(ap.pv[0], zt, fmaf(ap.pv[1], yt, fmaf(ap.pv[2], xt, ap.pv[3])));
+  const float nw = fmaf(ap.pw[0], zt, fmaf(ap.pw[1], yt, fmaf(ap.pw[2], xt, ap.pw[3])));
+  float umin = 3.0e38f, umax = -3.0e38f, vmin = 3.0e38f, vmax = -3.0e38f;
+  bool ok = true;
+#pragma unroll
+  for (int c = 0; c < 4; ++c) {
+    const float da = (c & 1) ? 1.0f : -1.0f, db = (c & 2) ? 1.0f : -1.0f;
+    const float cu = fmaf(da, ap.pu[ap.a], fmaf(db, ap.pu[ap.b], nu));
+    const float cv = fmaf(da, ap.pv[ap.a], fmaf(db, ap.pv[ap.b], nv));
+    const float cw = fmaf(da, ap.pw[ap.a], fmaf(db, ap.pw[ap.b], nw));
+    ok = ok && cw > 0.0f;
+    const float u = cu / cw, v = cv / cw;
+    umin = fminf(umin, u);
+    umax = fmaxf(umax, u);
+    vmin = fminf(vmin, v);
+    vmax = fmaxf(vmax, v);
+  }
+  if (!ok || !(umin <= umax) || !(vmin <= vmax)) return acc;
+  const int iu_lo = max(0, (int)floorf(clamp_coord(umin)) + 1 + g.ou);
+  const int iu_hi = min(g.cols - 1, (int)ceilf(clamp_coord(umax)) - 1 + g.ou);
+  const int iv_lo = max(0, (int)floorf(clamp_coord(vmin)) + 1 + g.ov);
+  const int iv_hi = min(g.rows - 1, (int)ceilf(clamp_coord(vmax)) - 1 + g.ov);
+  for (int iv = iv_lo; iv <= iv_hi; ++iv) {
+    for (int iu = iu_lo; iu <= iu_hi; ++iu) {
+      const Ray r = pixel_ray(ap, columns, g, theta, iu, iv);
+      const float wa = tent(fmaf(kt, r.ma, r.Xa) - it);
+      const float wb = tent(fmaf(kt, r.mb, r.Xb) - jt);
+      const float w = wa * wb;
+      if (w > 0.0f) acc = fmaf(w, __ldg(base + iv * pv.s_row + iu * pv.s_col).x, acc);
+    }
+  }
+  return acc;
+}
+
+// One thread per voxel; any geometry (the tuning's bp_general = 1).
 __global__ void __launch_bounds__(128)
     bp_general_kernel(const AngleParams* __restrict__ params,
                       const ColumnEntry* __restrict__ columns, const int* __restrict__ angles,
@@ -350,61 +423,246 @@ __global__ void __launch_bounds__(128)
   const int z = blockIdx.z;
   if (x >= g.nx || y >= g.ny) return;
   const float xt = float(x - g.ox), yt = float(y - g.oy), zt = float(z - g.oz);
-  // pair (iv, theta, iu) at base + iv * s_row + iu * s_col: row-major
-  // (rows nangles * cols apart) or column-major (rows adjacent)
-  const size_t RP = size_t(g.rows + 2 * kRowPad);
-  const size_t s_row = zlayout ? 1 : (size_t)g.nangles * g.cols;
-  const size_t s_col = zlayout ? RP : 1;
+  const PairView pv(g, zlayout);
   float acc = 0.0f;
   for (int n = 0; n < n_angles; ++n) {
     const int theta = __ldg(angles + n);
-    const AngleParams& ap = params[theta];
-    const float kt = coord(ap.d, zt, yt, xt);
-    const float it = coord(ap.a, zt, yt, xt);
-    const float jt = coord(ap.b, zt, yt, xt);
-    // Project the four corners (kt, it -+ 1, jt -+ 1) of the tent footprint.
-    const float nu = fmaf(ap.pu[0], zt, fmaf(ap.pu[1], yt, fmaf(ap.pu[2], xt, ap.pu[3])));
-    const float nv = fmaf(ap.pv[0], zt, fmaf(ap.pv[1], yt, fmaf(ap.pv[2], xt, ap.pv[3])));
-    const float nw = fmaf(ap.pw[0], zt, fmaf(ap.pw[1], yt, fmaf(ap.pw[2], xt, ap.pw[3])));
-    float umin = 3.0e38f, umax = -3.0e38f, vmin = 3.0e38f, vmax = -3.0e38f;
-    bool ok = true;
-#pragma unroll
-    for (int c = 0; c < 4; ++c) {
-      const float da = (c & 1) ? 1.0f : -1.0f, db = (c & 2) ? 1.0f : -1.0f;
-      const float cu = fmaf(da, ap.pu[ap.a], fmaf(db, ap.pu[ap.b], nu));
-      const float cv = fmaf(da, ap.pv[ap.a], fmaf(db, ap.pv[ap.b], nv));
-      const float cw = fmaf(da, ap.pw[ap.a], fmaf(db, ap.pw[ap.b], nw));
-      ok = ok && cw > 0.0f;
-      const float u = cu / cw, v = cv / cw;
-      umin = fminf(umin, u);
-      umax = fmaxf(umax, u);
-      vmin = fminf(vmin, v);
-      vmax = fmaxf(vmax, v);
-    }
-    if (!ok || !(umin <= umax) || !(vmin <= vmax)) continue;
-    const int iu_lo = max(0, (int)floorf(clamp_coord(umin)) + 1 + g.ou);
-    const int iu_hi = min(g.cols - 1, (int)ceilf(clamp_coord(umax)) - 1 + g.ou);
-    const int iv_lo = max(0, (int)floorf(clamp_coord(vmin)) + 1 + g.ov);
-    const int iv_hi = min(g.rows - 1, (int)ceilf(clamp_coord(vmax)) - 1 + g.ov);
-    const float2* base = zlayout ? sinow + (size_t)theta * g.cols * RP + kRowPad
-                                 : sinow + ((size_t)kRowPad * g.nangles + theta) * g.cols;
-    for (int iv = iv_lo; iv <= iv_hi; ++iv) {
-      const float vt = float(iv - g.ov);
-      for (int iu = iu_lo; iu <= iu_hi; ++iu) {
-        const Ray r = ap.separable ? ray_column(columns[(size_t)theta * g.cols + iu], vt)
-                                   : ray_general(ap, float(iu - g.ou), vt);
-        const float wa = tent(fmaf(kt, r.ma, r.Xa) - it);
-        const float wb = tent(fmaf(kt, r.mb, r.Xb) - jt);
-        const float w = wa * wb;
-        if (w > 0.0f) acc = fmaf(w, __ldg(base + iv * s_row + iu * s_col).x, acc);
-      }
-    }
+    acc = general_voxel_terms(params[theta], columns, pv.base(sinow, g, theta, zlayout), pv, g,
+                              theta, zt, yt, xt, acc);
   }
   float* out = vol + ((size_t)z * g.ny + y) * g.nx + x;
   if (additive)
     *out += acc;
   else
     *out = acc;
+}
+
+// ------------------------------------------------- general, staged per box
+// The same sums computed by blocks that own a box of voxels and, per angle,
+// stage the rays of the detector region the box projects to in shared memory.
+// A pixel's ray (a reciprocal and eight multiply-adds) and its weighted value
+// are then computed and loaded once per box instead of once per voxel whose
+// footprint box contains it. Each voxel bounds its footprint from its centre's
+// projection (below) and sums the same candidates, with the same weights, in
+// the same order as general_voxel_terms (pixels whose weight is 0 add
+// nothing), so both give the same result. Where a region would not fit (a
+// detector much finer than the voxels, or a source inside the box's reach), the
+// box falls back to general_voxel_terms for that angle.
+constexpr int kGenBoxZ = 16, kGenBoxY = 8, kGenBoxX = 8;  // voxels per block
+constexpr int kGenRunX = 4;                               // voxels along x per thread
+constexpr int kGenThreads = kGenBoxZ * kGenBoxY * kGenBoxX / kGenRunX;  // 256
+constexpr int kGenStage = 2048;                           // staged pixels per angle
+
+// Detector region of one (box, angle): columns u0 .. u0+nu-1, rows v0 ..
+// v0+nv-1; pixel (iu, iv) is staged at (iu - u0) * su + (iv - v0) * sv.
+// mode 0: no pixel reaches the box; 1: staged; 2: per-voxel fallback.
+struct GenRegion {
+  int u0, v0, nu, nv, su, sv, mode, pad;
+};
+
+// Region of the box [lo, hi] (anchored z, y, x) for one angle, computed by the
+// 32 lanes of one warp: lanes 0-7 project the corners of the box widened by
+// one voxel (the tent's half-width) along a and b; the projection of the
+// box is the convex hull of theirs when every corner lies in front of the
+// source (w > 0, an affine function of the position). One pixel of margin on
+// each side covers rounding.
+__device__ __forceinline__ void gen_region(const AngleParams& ap, const DeviceGeometry& g,
+                                           const float (&lo)[3], const float (&hi)[3],
+                                           int zlayout, GenRegion* out) {
+  const int lane = threadIdx.x & 31;
+  float umin = 3.0e38f, umax = -3.0e38f, vmin = 3.0e38f, vmax = -3.0e38f;
+  int bad = 0;
+  if (lane < 8) {
+    float P[3];
+#pragma unroll
+    for (int ax = 0; ax < 3; ++ax) {
+      const float e = ax == ap.d ? 0.0f : 1.0f;
+      P[ax] = ((lane >> ax) & 1) ? hi[ax] + e : lo[ax] - e;
+    }
+    const float nu = fmaf(ap.pu[0], P[0], fmaf(ap.pu[1], P[1], fmaf(ap.pu[2], P[2], ap.pu[3])));
+    const float nv = fmaf(ap.pv[0], P[0], fmaf(ap.pv[1], P[1], fmaf(ap.pv[2], P[2], ap.pv[3])));
+    const float nw = fmaf(ap.pw[0], P[0], fmaf(ap.pw[1], P[1], fmaf(ap.pw[2], P[2], ap.pw[3])));
+    const float u = nu / nw, v = nv / nw;
+    if (!(nw > 0.0f) || !isfinite(u) || !isfinite(v)) {
+      bad = 1;
+    } else {
+      umin = umax = u;
+      vmin = vmax = v;
+    }
+  }
+#pragma unroll
+  for (int o = 4; o >= 1; o >>= 1) {  // lanes 0-7 exchange among themselves
+    umin = fminf(umin, __shfl_xor_sync(0xffffffffu, umin, o));
+    umax = fmaxf(umax, __shfl_xor_sync(0xffffffffu, umax, o));
+    vmin = fminf(vmin, __shfl_xor_sync(0xffffffffu, vmin, o));
+    vmax = fmaxf(vmax, __shfl_xor_sync(0xffffffffu, vmax, o));
+    bad |= __shfl_xor_sync(0xffffffffu, bad, o);
+  }
+  if (lane != 0) return;
+  GenRegion r{};
+  if (bad) {
+    r.mode = 2;
+  } else {
+    const int u0 = max(0, (int)floorf(clamp_coord(umin)) + g.ou);
+    const int u1 = min(g.cols - 1, (int)ceilf(clamp_coord(umax)) + g.ou);
+    const int v0 = max(0, (int)floorf(clamp_coord(vmin)) + g.ov);
+    const int v1 = min(g.rows - 1, (int)ceilf(clamp_coord(vmax)) + g.ov);
+    r.u0 = u0;
+    r.v0 = v0;
+    r.nu = u1 - u0 + 1;
+    r.nv = v1 - v0 + 1;
+    if (r.nu <= 0 || r.nv <= 0)
+      r.mode = 0;
+    else if ((long long)r.nu * r.nv > kGenStage)
+      r.mode = 2;
+    else
+      r.mode = 1;
+    // staged in the sinogram's own order, so the staging reads are coalesced
+    r.su = zlayout ? r.nv : 1;
+    r.sv = zlayout ? 1 : r.nu;
+  }
+  *out = r;
+}
+
+__global__ void __launch_bounds__(kGenThreads, 4)
+    bp_general_box_kernel(const AngleParams* __restrict__ params,
+                          const ColumnEntry* __restrict__ columns,
+                          const int* __restrict__ angles, int n_angles,
+                          const float2* __restrict__ sinow, float* __restrict__ vol,
+                          DeviceGeometry g, int additive, int zlayout) {
+  __shared__ float4 s_ray[kGenStage];  // Xa, ma, Xb, mb
+  __shared__ float s_val[kGenStage];   // W y
+  __shared__ GenRegion s_reg[2];       // regions of angles n and n + 1
+  const int tid = threadIdx.x, warp = tid >> 5;
+  const int bz = blockIdx.z * kGenBoxZ, by = blockIdx.y * kGenBoxY, bx = blockIdx.x * kGenBoxX;
+  // this thread's voxels: (z, y, x0 + m), m < kGenRunX
+  const int z = bz + (tid & 15), y = by + (tid >> 5), x0 = bx + ((tid >> 4) & 1) * kGenRunX;
+  const bool zy_in = z < g.nz && y < g.ny;
+  const float zt = float(z - g.oz), yt = float(y - g.oy);
+  // the box, clipped to the volume, in anchored coordinates (z, y, x)
+  const float lo[3] = {float(bz - g.oz), float(by - g.oy), float(bx - g.ox)};
+  const float hi[3] = {float(min(bz + kGenBoxZ, g.nz) - 1 - g.oz),
+                       float(min(by + kGenBoxY, g.ny) - 1 - g.oy),
+                       float(min(bx + kGenBoxX, g.nx) - 1 - g.ox)};
+  const PairView pv(g, zlayout);
+  float acc[kGenRunX];
+#pragma unroll
+  for (int m = 0; m < kGenRunX; ++m) acc[m] = 0.0f;
+  if (warp == 0 && n_angles > 0) gen_region(params[__ldg(angles)], g, lo, hi, zlayout, &s_reg[0]);
+  __syncthreads();
+  for (int n = 0; n < n_angles; ++n) {
+    const int theta = __ldg(angles + n);
+    const AngleParams& ap = params[theta];
+    const GenRegion R = s_reg[n & 1];
+    const float2* __restrict__ base = pv.base(sinow, g, theta, zlayout);
+    if (R.mode == 1) {
+      // stage the region: pixel s = du * su + dv * sv, walked in storage order
+      const int inner = zlayout ? R.nv : R.nu, total = R.nu * R.nv;
+      const int step_q = kGenThreads / inner, step_r = kGenThreads % inner;
+      int q = tid / inner, r = tid % inner;
+      for (int s = tid; s < total; s += kGenThreads) {
+        const int iu = R.u0 + (zlayout ? q : r), iv = R.v0 + (zlayout ? r : q);
+        const Ray ray = pixel_ray(ap, columns, g, theta, iu, iv);
+        s_ray[s] = make_float4(ray.Xa, ray.ma, ray.Xb, ray.mb);
+        s_val[s] = __ldg(base + iv * pv.s_row + iu * pv.s_col).x;
+        q += step_q;
+        r += step_r;
+        if (r >= inner) {
+          r -= inner;
+          ++q;
+        }
+      }
+    }
+    __syncthreads();
+    // the next angle's region, into the slot angle n - 1 used
+    if (warp == 0 && n + 1 < n_angles)
+      gen_region(params[__ldg(angles + n + 1)], g, lo, hi, zlayout, &s_reg[(n + 1) & 1]);
+    if (zy_in && R.mode == 1) {
+      // Footprint bound from the centre's projection (u*, v*) = (nu, nv) / nw:
+      // a corner (+-1 along a and b) moves the numerators by du, dv and the
+      // denominator by dw, and moves u by (du - u* dw) / (nw + dw), at most
+      // (|pu_a| + |pu_b| + |u*| (|pw_a| + |pw_b|)) / (nw - |pw_a| - |pw_b|),
+      // where nw - |pw_a| - |pw_b| is the smallest corner's w.
+      const float Su = fabsf(ap.pu[ap.a]) + fabsf(ap.pu[ap.b]);
+      const float Sv = fabsf(ap.pv[ap.a]) + fabsf(ap.pv[ap.b]);
+      const float Ew = fabsf(ap.pw[ap.a]) + fabsf(ap.pw[ap.b]);
+      const int u_last = R.u0 + R.nu - 1, v_last = R.v0 + R.nv - 1;
+#pragma unroll
+      for (int m = 0; m < kGenRunX; ++m) {
+        if (x0 + m >= g.nx) break;
+        const float xt = float(x0 + m - g.ox);
+        const float kt = coord(ap.d, zt, yt, xt);
+        const float it = coord(ap.a, zt, yt, xt);
+        const float jt = coord(ap.b, zt, yt, xt);
+        const float nu = fmaf(ap.pu[0], zt, fmaf(ap.pu[1], yt, fmaf(ap.pu[2], xt, ap.pu[3])));
+        const float nv = fmaf(ap.pv[0], zt, fmaf(ap.pv[1], yt, fmaf(ap.pv[2], xt, ap.pv[3])));
+        const float nw = fmaf(ap.pw[0], zt, fmaf(ap.pw[1], yt, fmaf(ap.pw[2], xt, ap.pw[3])));
+        const float rw = __fdividef(1.0f, nw), rm = __fdividef(1.0f, nw - Ew);
+        const float us = nu * rw, vs = nv * rw;
+        // the bound plus a margin for the rounding of both computations
+        const float du = fmaf(fmaf(fabsf(us), Ew, Su), rm, fmaf(1e-5f, fabsf(us), 1e-2f));
+        const float dv = fmaf(fmaf(fabsf(vs), Ew, Sv), rm, fmaf(1e-5f, fabsf(vs), 1e-2f));
+        int iu_lo = R.u0, iu_hi = u_last, iv_lo = R.v0, iv_hi = v_last;
+        if (nw - Ew > 0.0f) {  // (else: the whole region, clamped below)
+          iu_lo = max(iu_lo, (int)floorf(clamp_coord(us - du)) + 1 + g.ou);
+          iu_hi = min(iu_hi, (int)ceilf(clamp_coord(us + du)) - 1 + g.ou);
+          iv_lo = max(iv_lo, (int)floorf(clamp_coord(vs - dv)) + 1 + g.ov);
+          iv_hi = min(iv_hi, (int)ceilf(clamp_coord(vs + dv)) - 1 + g.ov);
+        }
+        float a = acc[m];
+        for (int iv = iv_lo; iv <= iv_hi; ++iv) {
+          const int row = (iv - R.v0) * R.sv - R.u0 * R.su;
+          for (int iu = iu_lo; iu <= iu_hi; ++iu) {
+            const int s = row + iu * R.su;
+            const float4 r4 = s_ray[s];
+            const float wa = tent(fmaf(kt, r4.y, r4.x) - it);
+            const float wb = tent(fmaf(kt, r4.w, r4.z) - jt);
+            const float w = wa * wb;
+            if (w > 0.0f) a = fmaf(w, s_val[s], a);
+          }
+        }
+        acc[m] = a;
+      }
+    } else if (zy_in && R.mode == 2) {
+#pragma unroll
+      for (int m = 0; m < kGenRunX; ++m)
+        if (x0 + m < g.nx)
+          acc[m] = general_voxel_terms(ap, columns, base, pv, g, theta, zt, yt,
+                                       float(x0 + m - g.ox), acc[m]);
+    }
+    __syncthreads();  // stage reused and next region visible
+  }
+  if (!zy_in) return;
+#pragma unroll
+  for (int m = 0; m < kGenRunX; ++m) {
+    if (x0 + m >= g.nx) break;
+    float* out = vol + ((size_t)z * g.ny + y) * g.nx + x0 + m;
+    if (additive)
+      *out += acc[m];
+    else
+      *out = acc[m];
+  }
+}
+
+// Matched backprojection of the n general angles at `angles` (device) into
+// vol (= or +=), from the row-pair sinogram `pairs` (column-major if zlayout).
+// n = 0 with additive = 0 writes zeros. The tuning's bp_general picks the
+// box kernel (0) or one thread per voxel (1); both compute the same sums.
+void launch_bp_general(const tsgb_projector* p, const int* angles, int n, const float2* pairs,
+                       float* vol, bool additive, bool zlayout, cudaStream_t stream) {
+  const DeviceGeometry& g = p->g;
+  if (p->tuning.bp_general == 1) {
+    const dim3 grid((g.nx + 31) / 32, (g.ny + 3) / 4, g.nz);
+    bp_general_kernel<<<grid, dim3(32, 4), 0, stream>>>(p->d_params, p->d_columns, angles, n,
+                                                        pairs, vol, g, additive ? 1 : 0,
+                                                        zlayout ? 1 : 0);
+    return;
+  }
+  const dim3 grid((g.nx + kGenBoxX - 1) / kGenBoxX, (g.ny + kGenBoxY - 1) / kGenBoxY,
+                  (g.nz + kGenBoxZ - 1) / kGenBoxZ);
+  bp_general_box_kernel<<<grid, kGenThreads, 0, stream>>>(p->d_params, p->d_columns, angles, n,
+                                                          pairs, vol, g, additive ? 1 : 0,
+                                                          zlayout ? 1 : 0);
 }
 
 // Bilinear detector value at anchored (ut, vt), zero outside the detector.
@@ -764,12 +1022,9 @@ int launch_bp_matched(const tsgb_projector* p, float* vol, const float* sino, bo
     float* volt = reinterpret_cast<float*>(reinterpret_cast<char*>(workspace) + bp_pairs_bytes(g));
     const bool written = launch_bp_zlane_separable(p, off_x, n_ax, off_y, n_ay, workspace, volt, vol,
                                                    additive ? 1 : 0, nullptr, stream);
-    if (n_g > 0 || (!written && !additive)) {
-      const dim3 grid((g.nx + 31) / 32, (g.ny + 3) / 4, g.nz);
-      bp_general_kernel<<<grid, dim3(32, 4), 0, stream>>>(p->d_params, p->d_columns,
-                                                          p->d_gen_angles + off_g, n_g, pairs, vol,
-                                                          g, (additive || written) ? 1 : 0, 1);
-    }
+    if (n_g > 0 || (!written && !additive))
+      launch_bp_general(p, p->d_gen_angles + off_g, n_g, pairs, vol, additive || written, true,
+                        stream);
     return int(cudaGetLastError());
   }
   const size_t rs = (size_t)g.nangles * g.cols;  // elements between rows
@@ -796,13 +1051,9 @@ int launch_bp_matched(const tsgb_projector* p, float* vol, const float* sino, bo
     launch_sep_pass(p, false, p->d_sep_angles + off_y, n_ay,
                     (additive || n_ax > 0) ? kBpAdd : kBpSet, pairs, vol, nullptr, nullptr, stream);
   const bool written = n_ax + n_ay > 0;
-  if (n_g > 0 || (!written && !additive)) {
-    const dim3 block(32, 4);
-    const dim3 grid((g.nx + 31) / 32, (g.ny + 3) / 4, g.nz);
-    bp_general_kernel<<<grid, block, 0, stream>>>(p->d_params, p->d_columns,
-                                                  p->d_gen_angles + off_g, n_g, pairs, vol, g,
-                                                  (additive || written) ? 1 : 0, 0);
-  }
+  if (n_g > 0 || (!written && !additive))
+    launch_bp_general(p, p->d_gen_angles + off_g, n_g, pairs, vol, additive || written, false,
+                      stream);
   return int(cudaGetLastError());
 }
 
@@ -845,10 +1096,8 @@ int launch_bp_sirt(const tsgb_projector* p, float* vol, const float* C, const fl
                         vsum, nullptr, nullptr, stream);
       written = n_ax + n_ay > 0;
     }
-    const dim3 grid((g.nx + 31) / 32, (g.ny + 3) / 4, g.nz);
-    bp_general_kernel<<<grid, dim3(32, 4), 0, stream>>>(p->d_params, p->d_columns, p->d_gen_angles,
-                                                        p->n_general_bp, pairs, vsum, g,
-                                                        written ? 1 : 0, bp_uses_zlane(p) ? 1 : 0);
+    launch_bp_general(p, p->d_gen_angles, p->n_general_bp, pairs, vsum, written,
+                      bp_uses_zlane(p), stream);
     const long long n = (long long)g.nz * g.ny * g.nx;
     const long long blocks = (n + 255) / 256;
     sirt_update_kernel<<<int(blocks < 152LL * 32 ? blocks : 152LL * 32), 256, 0, stream>>>(

@@ -402,8 +402,9 @@ int tsgb_projector_set_tuning(tsgb_projector* p, const tsgb_tuning* t) {
     return fail(TSGB_ERR_INVALID, "fp_pair_layout must be 0 or 1");
   if (t->bp_kernel != 0 && t->bp_kernel != 1) return fail(TSGB_ERR_INVALID, "bp_kernel must be 0 or 1");
   if (t->bp_shape < 0 || t->bp_shape > 6) return fail(TSGB_ERR_INVALID, "bp_shape must lie in 0 .. 6");
-  for (int i = 0; i < 2; ++i)
-    if (t->reserved[i] != 0) return fail(TSGB_ERR_INVALID, "reserved tuning fields must be 0");
+  if (t->bp_general != 0 && t->bp_general != 1)
+    return fail(TSGB_ERR_INVALID, "bp_general must be 0 or 1");
+  if (t->reserved != 0) return fail(TSGB_ERR_INVALID, "reserved tuning fields must be 0");
   // the projector that runs the FP and the matched BP
   (p->fine ? p->fine : p)->tuning = *t;
   return TSGB_OK;

@@ -106,7 +106,7 @@ class Projector:
         return dict(zip(keys, [int(v) for v in out]))
 
     TUNING_KEYS = ("fp_patch_rows", "fp_patch_cols", "fp_group_pairs", "fp_pair_layout",
-                   "bp_kernel", "bp_shape")
+                   "bp_kernel", "bp_shape", "bp_general")
 
     def get_tuning(self, device_index=None):
         """Launch schedule of the forward projector (see tsgb_tuning)."""
