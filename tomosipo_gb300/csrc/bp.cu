@@ -454,7 +454,8 @@ constexpr int kGenThreads = kGenBoxZ * kGenBoxY * kGenBoxX / kGenRunX;  // 256
 constexpr int kGenStage = 2048;                           // staged pixels per angle
 
 // Detector region of one (box, angle): columns u0 .. u0+nu-1, rows v0 ..
-// v0+nv-1; pixel (iu, iv) is staged at (iu - u0) * su + (iv - v0) * sv.
+// v0+nv-1; pixel (iu, iv) is staged at (iu - u0) * su + (iv - v0) * sv
+// (su = 1 or sv = 1: the sinogram's own order).
 // mode 0: no pixel reaches the box; 1: staged; 2: per-voxel fallback.
 struct GenRegion {
   int u0, v0, nu, nv, su, sv, mode, pad;
@@ -511,15 +512,19 @@ __device__ __forceinline__ void gen_region(const AngleParams& ap, const DeviceGe
     r.v0 = v0;
     r.nu = u1 - u0 + 1;
     r.nv = v1 - v0 + 1;
+    // staged in the sinogram's own order, so the staging reads are coalesced,
+    // with an odd stride between columns (rows) so that the two half-warps,
+    // four voxels apart along x, read different banks
+    const int inner = zlayout ? r.nv : r.nu, outer = zlayout ? r.nu : r.nv;
+    const int stride = inner | 1;
     if (r.nu <= 0 || r.nv <= 0)
       r.mode = 0;
-    else if ((long long)r.nu * r.nv > kGenStage)
+    else if ((long long)outer * stride > kGenStage)
       r.mode = 2;
     else
       r.mode = 1;
-    // staged in the sinogram's own order, so the staging reads are coalesced
-    r.su = zlayout ? r.nv : 1;
-    r.sv = zlayout ? 1 : r.nu;
+    r.su = zlayout ? stride : 1;
+    r.sv = zlayout ? 1 : stride;
   }
   *out = r;
 }
@@ -550,21 +555,32 @@ __global__ void __launch_bounds__(kGenThreads, 4)
   for (int m = 0; m < kGenRunX; ++m) acc[m] = 0.0f;
   if (warp == 0 && n_angles > 0) gen_region(params[__ldg(angles)], g, lo, hi, zlayout, &s_reg[0]);
   __syncthreads();
+  const float xt0 = float(x0 - g.ox);
   for (int n = 0; n < n_angles; ++n) {
     const int theta = __ldg(angles + n);
     const AngleParams& ap = params[theta];
     const GenRegion R = s_reg[n & 1];
     const float2* __restrict__ base = pv.base(sinow, g, theta, zlayout);
-    if (R.mode == 1) {
-      // stage the region: pixel s = du * su + dv * sv, walked in storage order
+    if (warp == 0) {
+      // the next angle's region, into the slot angle n - 1 used, while the
+      // other warps stage this one
+      if (n + 1 < n_angles)
+        gen_region(params[__ldg(angles + n + 1)], g, lo, hi, zlayout, &s_reg[(n + 1) & 1]);
+    } else if (R.mode == 1) {
+      // stage the region (warps 1 .. 7): pixel (du, dv) at du * su + dv * sv,
+      // walked in storage order
+      constexpr int kStagers = kGenThreads - 32;
       const int inner = zlayout ? R.nv : R.nu, total = R.nu * R.nv;
-      const int step_q = kGenThreads / inner, step_r = kGenThreads % inner;
-      int q = tid / inner, r = tid % inner;
-      for (int s = tid; s < total; s += kGenThreads) {
+      const int stride = zlayout ? R.su : R.sv;
+      const int t0 = tid - 32;
+      const int step_q = kStagers / inner, step_r = kStagers % inner;
+      int q = t0 / inner, r = t0 % inner;
+      for (int t = t0; t < total; t += kStagers) {
         const int iu = R.u0 + (zlayout ? q : r), iv = R.v0 + (zlayout ? r : q);
         const Ray ray = pixel_ray(ap, columns, g, theta, iu, iv);
-        s_ray[s] = make_float4(ray.Xa, ray.ma, ray.Xb, ray.mb);
-        s_val[s] = __ldg(base + iv * pv.s_row + iu * pv.s_col).x;
+        const int st = q * stride + r;
+        s_ray[st] = make_float4(ray.Xa, ray.ma, ray.Xb, ray.mb);
+        s_val[st] = __ldg(base + iv * pv.s_row + iu * pv.s_col).x;
         q += step_q;
         r += step_r;
         if (r >= inner) {
@@ -574,54 +590,68 @@ __global__ void __launch_bounds__(kGenThreads, 4)
       }
     }
     __syncthreads();
-    // the next angle's region, into the slot angle n - 1 used
-    if (warp == 0 && n + 1 < n_angles)
-      gen_region(params[__ldg(angles + n + 1)], g, lo, hi, zlayout, &s_reg[(n + 1) & 1]);
     if (zy_in && R.mode == 1) {
+      // The thread's voxels run along x, which is one of the angle's axes
+      // d, a, b: their (kt, it, jt) step by 1 along that one.
+      const int d = ap.d, a = ap.a;
+      const float kt0 = d == 0 ? zt : (d == 1 ? yt : xt0);
+      const float it0 = a == 0 ? zt : (a == 1 ? yt : xt0);
+      const float jt0 = (d != 0 && a != 0) ? zt : ((d != 1 && a != 1) ? yt : xt0);
+      const float dk = d == 2 ? 1.0f : 0.0f, di = a == 2 ? 1.0f : 0.0f;
+      const float dj = 1.0f - dk - di;
       // Footprint bound from the centre's projection (u*, v*) = (nu, nv) / nw:
       // a corner (+-1 along a and b) moves the numerators by du, dv and the
       // denominator by dw, and moves u by (du - u* dw) / (nw + dw), at most
       // (|pu_a| + |pu_b| + |u*| (|pw_a| + |pw_b|)) / (nw - |pw_a| - |pw_b|),
       // where nw - |pw_a| - |pw_b| is the smallest corner's w.
-      const float Su = fabsf(ap.pu[ap.a]) + fabsf(ap.pu[ap.b]);
-      const float Sv = fabsf(ap.pv[ap.a]) + fabsf(ap.pv[ap.b]);
-      const float Ew = fabsf(ap.pw[ap.a]) + fabsf(ap.pw[ap.b]);
+      const float Su = fabsf(ap.pu[a]) + fabsf(ap.pu[ap.b]);
+      const float Sv = fabsf(ap.pv[a]) + fabsf(ap.pv[ap.b]);
+      const float Ew = fabsf(ap.pw[a]) + fabsf(ap.pw[ap.b]);
+      const float nu0 = fmaf(ap.pu[0], zt, fmaf(ap.pu[1], yt, fmaf(ap.pu[2], xt0, ap.pu[3])));
+      const float nv0 = fmaf(ap.pv[0], zt, fmaf(ap.pv[1], yt, fmaf(ap.pv[2], xt0, ap.pv[3])));
+      const float nw0 = fmaf(ap.pw[0], zt, fmaf(ap.pw[1], yt, fmaf(ap.pw[2], xt0, ap.pw[3])));
+      const float pu2 = ap.pu[2], pv2 = ap.pv[2], pw2 = ap.pw[2];
+      // pixel index = anchored coordinate + anchor; the first pixel above a
+      // bound t is floor(t) + 1, the last below it ceil(t) - 1
+      const float lo_u = float(1 + g.ou), hi_u = float(g.ou - 1);
+      const float lo_v = float(1 + g.ov), hi_v = float(g.ov - 1);
       const int u_last = R.u0 + R.nu - 1, v_last = R.v0 + R.nv - 1;
 #pragma unroll
       for (int m = 0; m < kGenRunX; ++m) {
         if (x0 + m >= g.nx) break;
-        const float xt = float(x0 + m - g.ox);
-        const float kt = coord(ap.d, zt, yt, xt);
-        const float it = coord(ap.a, zt, yt, xt);
-        const float jt = coord(ap.b, zt, yt, xt);
-        const float nu = fmaf(ap.pu[0], zt, fmaf(ap.pu[1], yt, fmaf(ap.pu[2], xt, ap.pu[3])));
-        const float nv = fmaf(ap.pv[0], zt, fmaf(ap.pv[1], yt, fmaf(ap.pv[2], xt, ap.pv[3])));
-        const float nw = fmaf(ap.pw[0], zt, fmaf(ap.pw[1], yt, fmaf(ap.pw[2], xt, ap.pw[3])));
+        const float fm = float(m);
+        const float kt = fmaf(fm, dk, kt0), it = fmaf(fm, di, it0), jt = fmaf(fm, dj, jt0);
+        const float nu = fmaf(fm, pu2, nu0), nv = fmaf(fm, pv2, nv0), nw = fmaf(fm, pw2, nw0);
         const float rw = __fdividef(1.0f, nw), rm = __fdividef(1.0f, nw - Ew);
         const float us = nu * rw, vs = nv * rw;
-        // the bound plus a margin for the rounding of both computations
+        // the bound plus a margin for the rounding of both computations; a
+        // pixel within the margin of the bound has weight 0, so rounding of
+        // the bound itself cannot drop a pixel that has weight
         const float du = fmaf(fmaf(fabsf(us), Ew, Su), rm, fmaf(1e-5f, fabsf(us), 1e-2f));
         const float dv = fmaf(fmaf(fabsf(vs), Ew, Sv), rm, fmaf(1e-5f, fabsf(vs), 1e-2f));
         int iu_lo = R.u0, iu_hi = u_last, iv_lo = R.v0, iv_hi = v_last;
-        if (nw - Ew > 0.0f) {  // (else: the whole region, clamped below)
-          iu_lo = max(iu_lo, (int)floorf(clamp_coord(us - du)) + 1 + g.ou);
-          iu_hi = min(iu_hi, (int)ceilf(clamp_coord(us + du)) - 1 + g.ou);
-          iv_lo = max(iv_lo, (int)floorf(clamp_coord(vs - dv)) + 1 + g.ov);
-          iv_hi = min(iv_hi, (int)ceilf(clamp_coord(vs + dv)) - 1 + g.ov);
+        if (nw - Ew > 0.0f) {  // (else: the whole region)
+          // float-to-int conversions saturate (NaN -> 0); the region bounds
+          // every index
+          iu_lo = max(iu_lo, __float2int_rd((us - du) + lo_u));
+          iu_hi = min(iu_hi, __float2int_ru((us + du) + hi_u));
+          iv_lo = max(iv_lo, __float2int_rd((vs - dv) + lo_v));
+          iv_hi = min(iv_hi, __float2int_ru((vs + dv) + hi_v));
         }
-        float a = acc[m];
+        float acc_m = acc[m];
         for (int iv = iv_lo; iv <= iv_hi; ++iv) {
           const int row = (iv - R.v0) * R.sv - R.u0 * R.su;
           for (int iu = iu_lo; iu <= iu_hi; ++iu) {
-            const int s = row + iu * R.su;
-            const float4 r4 = s_ray[s];
-            const float wa = tent(fmaf(kt, r4.y, r4.x) - it);
-            const float wb = tent(fmaf(kt, r4.w, r4.z) - jt);
-            const float w = wa * wb;
-            if (w > 0.0f) a = fmaf(w, s_val[s], a);
+            const int st = row + iu * R.su;
+            const float4 r4 = s_ray[st];
+            // tent(t) as one saturating add (1 - |t| <= 1; NaN saturates to
+            // 0); a weight of 0 adds nothing
+            const float wa = __saturatef(1.0f - fabsf(fmaf(kt, r4.y, r4.x) - it));
+            const float wb = __saturatef(1.0f - fabsf(fmaf(kt, r4.w, r4.z) - jt));
+            acc_m = fmaf(wa * wb, s_val[st], acc_m);
           }
         }
-        acc[m] = a;
+        acc[m] = acc_m;
       }
     } else if (zy_in && R.mode == 2) {
 #pragma unroll
