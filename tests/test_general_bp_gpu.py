@@ -9,8 +9,10 @@ is within a rounding step of zero; the gate between them is 1e-7 relative L2.
 Cases cover both weighted-sinogram layouts (bp_kernel 0: row-major pairs,
 1: column-major), the additive form, volumes that are not whole boxes, a scan
 that mixes separable and tilted angles (the general kernel adds onto the
-separable passes), and a detector fine enough that the staged region
-does not fit and every box falls back to the per-voxel sums.
+separable passes), and the box kernel's three ways of summing: a box-wide
+window of candidate pixels (pixels about as large as voxels), a bound per
+voxel (footprints wider than that window), and, for a detector fine enough
+that the staged region does not fit, the per-voxel sums.
 """
 import numpy as np
 import pytest
@@ -40,6 +42,13 @@ def _cases():
         ),
         "mixed_separable_and_tilted": (
             vg32, ts.concatenate([cone.to_vec()[:6], (R * cone.to_vec())[6:]])),
+        # pixels ~2.5x finer than voxels: footprints wider than the box-wide
+        # window, so each voxel bounds its own (the region still fits)
+        "finer_detector_bounds": (
+            ts.volume(shape=24, size=1),
+            R * ts.cone(angles=5, shape=(60, 75), size=1.6, src_orig_dist=2.5,
+                        src_det_dist=3.5).to_vec(),
+        ),
         # pixels ~4x finer than voxels: a box's region exceeds the stage
         "fine_detector_fallback": (
             ts.volume(shape=24, size=1),

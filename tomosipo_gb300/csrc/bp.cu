@@ -452,14 +452,29 @@ constexpr int kGenBoxZ = 16, kGenBoxY = 8, kGenBoxX = 8;  // voxels per block
 constexpr int kGenRunX = 4;                               // voxels along x per thread
 constexpr int kGenThreads = kGenBoxZ * kGenBoxY * kGenBoxX / kGenRunX;  // 256
 constexpr int kGenStage = 2048;                           // staged pixels per angle
+constexpr int kGenWindow = 9;  // largest box-wide window (pixels) summed by every voxel
 
 // Detector region of one (box, angle): columns u0 .. u0+nu-1, rows v0 ..
 // v0+nv-1; pixel (iu, iv) is staged at (iu - u0) * su + (iv - v0) * sv
 // (su = 1 or sv = 1: the sinogram's own order).
-// mode 0: no pixel reaches the box; 1: staged; 2: per-voxel fallback.
+// mode 0: no pixel reaches the box; 1: staged, each voxel bounds its own
+// footprint; 3: staged, every voxel sums a window of wu x wv pixels from the
+// first above (u*, v*) - (hu, hv); 2: per-voxel fallback.
 struct GenRegion {
-  int u0, v0, nu, nv, su, sv, mode, pad;
+  int u0, v0, nu, nv, su, sv, mode, wu, wv;
+  float hu, hv;
 };
+
+// Half-extent bound of a voxel footprint's projection, in pixels: a corner
+// (+-1 along a and b) of the footprint moves the projection's numerators by
+// du (dv) and its denominator by dw, and moves u by (du - u* dw) / (nw + dw),
+// at most (S + |u*| E) / (nw - E) with S = |p_a| + |p_b| of that numerator and
+// E = |pw_a| + |pw_b| (nw - E is the smallest corner's w). The margin covers
+// the rounding of the bound and of the projection: pixels within it of the
+// bound have weight 0.
+__device__ __forceinline__ float footprint_half(float S, float E, float absu, float rm) {
+  return fmaf(fmaf(absu, E, S), rm, fmaf(1e-5f, absu, 1e-2f));
+}
 
 // Region of the box [lo, hi] (anchored z, y, x) for one angle, computed by the
 // 32 lanes of one warp: lanes 0-7 project the corners of the box widened by
@@ -471,7 +486,7 @@ __device__ __forceinline__ void gen_region(const AngleParams& ap, const DeviceGe
                                            const float (&lo)[3], const float (&hi)[3],
                                            int zlayout, GenRegion* out) {
   const int lane = threadIdx.x & 31;
-  float umin = 3.0e38f, umax = -3.0e38f, vmin = 3.0e38f, vmax = -3.0e38f;
+  float umin = 3.0e38f, umax = -3.0e38f, vmin = 3.0e38f, vmax = -3.0e38f, wmin = 3.0e38f;
   int bad = 0;
   if (lane < 8) {
     float P[3];
@@ -489,6 +504,7 @@ __device__ __forceinline__ void gen_region(const AngleParams& ap, const DeviceGe
     } else {
       umin = umax = u;
       vmin = vmax = v;
+      wmin = nw;
     }
   }
 #pragma unroll
@@ -497,6 +513,7 @@ __device__ __forceinline__ void gen_region(const AngleParams& ap, const DeviceGe
     umax = fmaxf(umax, __shfl_xor_sync(0xffffffffu, umax, o));
     vmin = fminf(vmin, __shfl_xor_sync(0xffffffffu, vmin, o));
     vmax = fmaxf(vmax, __shfl_xor_sync(0xffffffffu, vmax, o));
+    wmin = fminf(wmin, __shfl_xor_sync(0xffffffffu, wmin, o));
     bad |= __shfl_xor_sync(0xffffffffu, bad, o);
   }
   if (lane != 0) return;
@@ -525,6 +542,23 @@ __device__ __forceinline__ void gen_region(const AngleParams& ap, const DeviceGe
       r.mode = 1;
     r.su = zlayout ? stride : 1;
     r.sv = zlayout ? 1 : stride;
+    // One window for the whole box: every voxel centre lies inside the
+    // widened box, so its |u*|, |v*| and nw are bounded by the corners' (w is
+    // affine, u and v are monotone along lines), and so is its footprint
+    // bound. The pixels strictly inside (u* - hu, u* + hu) are at most
+    // ceil(2 hu) consecutive ones from floor(u* - hu) + 1.
+    const float E = fabsf(ap.pw[ap.a]) + fabsf(ap.pw[ap.b]);
+    if (r.mode == 1 && wmin - E > 0.0f) {
+      const float rm = 1.0f / (wmin - E);
+      r.hu = footprint_half(fabsf(ap.pu[ap.a]) + fabsf(ap.pu[ap.b]), E,
+                            fmaxf(fabsf(umin), fabsf(umax)), rm);
+      r.hv = footprint_half(fabsf(ap.pv[ap.a]) + fabsf(ap.pv[ap.b]), E,
+                            fmaxf(fabsf(vmin), fabsf(vmax)), rm);
+      r.wu = (int)ceilf(2.0f * r.hu);
+      r.wv = (int)ceilf(2.0f * r.hv);
+      if (r.wu >= 1 && r.wv >= 1 && r.wu * r.wv <= kGenWindow && r.wu <= r.nu && r.wv <= r.nv)
+        r.mode = 3;
+    }
   }
   *out = r;
 }
@@ -566,7 +600,7 @@ __global__ void __launch_bounds__(kGenThreads, 4)
       // other warps stage this one
       if (n + 1 < n_angles)
         gen_region(params[__ldg(angles + n + 1)], g, lo, hi, zlayout, &s_reg[(n + 1) & 1]);
-    } else if (R.mode == 1) {
+    } else if (R.mode == 1 || R.mode == 3) {
       // stage the region (warps 1 .. 7): pixel (du, dv) at du * su + dv * sv,
       // walked in storage order
       constexpr int kStagers = kGenThreads - 32;
@@ -590,7 +624,47 @@ __global__ void __launch_bounds__(kGenThreads, 4)
       }
     }
     __syncthreads();
-    if (zy_in && R.mode == 1) {
+    if (zy_in && R.mode == 3) {
+      // box-wide window: the same wu x wv candidates for every voxel, so
+      // the loops are uniform across the warp and need no per-voxel bound
+      const int d = ap.d, a = ap.a;
+      const float kt0 = d == 0 ? zt : (d == 1 ? yt : xt0);
+      const float it0 = a == 0 ? zt : (a == 1 ? yt : xt0);
+      const float jt0 = (d != 0 && a != 0) ? zt : ((d != 1 && a != 1) ? yt : xt0);
+      const float dk = d == 2 ? 1.0f : 0.0f, di = a == 2 ? 1.0f : 0.0f;
+      const float dj = 1.0f - dk - di;
+      const float nu0 = fmaf(ap.pu[0], zt, fmaf(ap.pu[1], yt, fmaf(ap.pu[2], xt0, ap.pu[3])));
+      const float nv0 = fmaf(ap.pv[0], zt, fmaf(ap.pv[1], yt, fmaf(ap.pv[2], xt0, ap.pv[3])));
+      const float nw0 = fmaf(ap.pw[0], zt, fmaf(ap.pw[1], yt, fmaf(ap.pw[2], xt0, ap.pw[3])));
+      const float pu2 = ap.pu[2], pv2 = ap.pv[2], pw2 = ap.pw[2];
+      // first pixel above u* - hu, as an index: floor(u* - hu) + 1 + anchor;
+      // the window is then moved inside the region if it sticks out (the
+      // footprint itself lies inside the region)
+      const float ou = float(1 + g.ou) - R.hu, ov = float(1 + g.ov) - R.hv;
+      const int u_first = R.u0 + R.nu - R.wu, v_first = R.v0 + R.nv - R.wv;
+#pragma unroll
+      for (int m = 0; m < kGenRunX; ++m) {
+        if (x0 + m >= g.nx) break;
+        const float fm = float(m);
+        const float kt = fmaf(fm, dk, kt0), it = fmaf(fm, di, it0), jt = fmaf(fm, dj, jt0);
+        const float rw = __fdividef(1.0f, fmaf(fm, pw2, nw0));
+        const float us = fmaf(fm, pu2, nu0) * rw, vs = fmaf(fm, pv2, nv0) * rw;
+        const int iu0 = min(max(__float2int_rd(us + ou), R.u0), u_first);
+        const int iv0 = min(max(__float2int_rd(vs + ov), R.v0), v_first);
+        const int st0 = (iv0 - R.v0) * R.sv + (iu0 - R.u0) * R.su;
+        float acc_m = acc[m];
+        for (int r = 0; r < R.wv; ++r) {
+          for (int c = 0; c < R.wu; ++c) {
+            const int st = st0 + r * R.sv + c * R.su;
+            const float4 r4 = s_ray[st];
+            const float wa = __saturatef(1.0f - fabsf(fmaf(kt, r4.y, r4.x) - it));
+            const float wb = __saturatef(1.0f - fabsf(fmaf(kt, r4.w, r4.z) - jt));
+            acc_m = fmaf(wa * wb, s_val[st], acc_m);
+          }
+        }
+        acc[m] = acc_m;
+      }
+    } else if (zy_in && R.mode == 1) {
       // The thread's voxels run along x, which is one of the angle's axes
       // d, a, b: their (kt, it, jt) step by 1 along that one.
       const int d = ap.d, a = ap.a;
@@ -599,11 +673,7 @@ __global__ void __launch_bounds__(kGenThreads, 4)
       const float jt0 = (d != 0 && a != 0) ? zt : ((d != 1 && a != 1) ? yt : xt0);
       const float dk = d == 2 ? 1.0f : 0.0f, di = a == 2 ? 1.0f : 0.0f;
       const float dj = 1.0f - dk - di;
-      // Footprint bound from the centre's projection (u*, v*) = (nu, nv) / nw:
-      // a corner (+-1 along a and b) moves the numerators by du, dv and the
-      // denominator by dw, and moves u by (du - u* dw) / (nw + dw), at most
-      // (|pu_a| + |pu_b| + |u*| (|pw_a| + |pw_b|)) / (nw - |pw_a| - |pw_b|),
-      // where nw - |pw_a| - |pw_b| is the smallest corner's w.
+      // footprint bound from the centre's projection (u*, v*) = (nu, nv) / nw
       const float Su = fabsf(ap.pu[a]) + fabsf(ap.pu[ap.b]);
       const float Sv = fabsf(ap.pv[a]) + fabsf(ap.pv[ap.b]);
       const float Ew = fabsf(ap.pw[a]) + fabsf(ap.pw[ap.b]);
@@ -624,11 +694,10 @@ __global__ void __launch_bounds__(kGenThreads, 4)
         const float nu = fmaf(fm, pu2, nu0), nv = fmaf(fm, pv2, nv0), nw = fmaf(fm, pw2, nw0);
         const float rw = __fdividef(1.0f, nw), rm = __fdividef(1.0f, nw - Ew);
         const float us = nu * rw, vs = nv * rw;
-        // the bound plus a margin for the rounding of both computations; a
-        // pixel within the margin of the bound has weight 0, so rounding of
-        // the bound itself cannot drop a pixel that has weight
-        const float du = fmaf(fmaf(fabsf(us), Ew, Su), rm, fmaf(1e-5f, fabsf(us), 1e-2f));
-        const float dv = fmaf(fmaf(fabsf(vs), Ew, Sv), rm, fmaf(1e-5f, fabsf(vs), 1e-2f));
+        // (rounding of the index computation moves a bound by far less than
+        // the margin, so it cannot drop a pixel that has weight)
+        const float du = footprint_half(Su, Ew, fabsf(us), rm);
+        const float dv = footprint_half(Sv, Ew, fabsf(vs), rm);
         int iu_lo = R.u0, iu_hi = u_last, iv_lo = R.v0, iv_hi = v_last;
         if (nw - Ew > 0.0f) {  // (else: the whole region)
           // float-to-int conversions saturate (NaN -> 0); the region bounds
