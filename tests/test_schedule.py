@@ -51,15 +51,18 @@ def test_pipeline_chunk_bounds(nang):
     """Angle chunks of a streamed projection cover every angle once, in order;
     the chunk whose transfer is exposed (the backprojection's first, the
     forward projection's last) is the smallest, and the rest grow by at most
-    PIPELINE_GROWTH from it."""
-    from tomosipo_gb300.projector import PIPELINE_GROWTH, _chunk_bounds
+    the direction's growth factor from it, the farthest also taking a
+    remainder smaller than one more step."""
+    from tomosipo_gb300.projector import PIPELINE_GROWTH_BP, PIPELINE_GROWTH_FP, _chunk_bounds
 
-    for forward in (False, True):
+    for forward, growth in ((False, PIPELINE_GROWTH_BP), (True, PIPELINE_GROWTH_FP)):
         b = [int(v) for v in _chunk_bounds(nang, forward)]
         sizes = np.diff(b)
         assert b[0] == 0 and b[-1] == nang and np.all(sizes >= 1)
         grow = sizes if not forward else sizes[::-1]
         assert grow[0] == min(sizes) <= max(1, nang // 32)
-        assert np.all(grow[1:] <= grow[:-1] * PIPELINE_GROWTH)
+        assert np.all(grow[1:-1] <= grow[:-2] * growth)
+        if len(grow) > 1:
+            assert grow[-1] < grow[-2] * growth * (growth + 1)
     assert list(_chunk_bounds(1024, False)) == [0, 32, 288, 1024]
-    assert list(_chunk_bounds(1024, True)) == [0, 736, 992, 1024]
+    assert list(_chunk_bounds(1024, True)) == [0, 544, 800, 928, 992, 1024]

@@ -183,11 +183,17 @@ def _as_device_tensor(arr, device, copy_in):
 # large (tsgb_direct_fp_angles / tsgb_direct_bp_angles / tsgb_copy_sino_angles).
 PIPELINE_MIN_BYTES = 256 << 20
 PIPELINE_MIN_ANGLES = 16
-# Chunk sizes grow by this factor from the chunk whose transfer is exposed:
-# a projection takes 15-20x longer per angle than its pinned transfer at
-# 512^3 (127-141 us against 7.5 us), so each chunk's transfer hides behind the
-# previous chunk's projection.
-PIPELINE_GROWTH = 8
+# Chunk sizes grow by these factors from the chunk whose transfer is exposed.
+# At full copy rates a projection takes 15-20x longer per angle than its
+# transfer at 512^3 (127-141 us against 7.5 us). Every backprojection chunk
+# rereads and rewrites the volume, so its chunks grow by 8: few chunks. A
+# forward chunk costs nothing extra (the volume copies are built once), and
+# downloads into host memory have measured as slow as 24 GB/s on a shared
+# host (193 GB/s otherwise), about twice the rate the forward projection
+# produces sinogram; chunks growing by 2 keep each download behind the
+# projection of the chunks after it even then.
+PIPELINE_GROWTH_BP = 8
+PIPELINE_GROWTH_FP = 2
 _copy_streams = {}
 
 
@@ -196,15 +202,19 @@ def _chunk_bounds(nang, forward):
 
     The backprojection's first chunk waits for its upload and the forward
     projection's last chunk for its download, so that chunk is small (1/32
-    of the angles) and the others grow geometrically away from it; every
-    backprojection chunk also rereads and rewrites the volume, so fewer
-    chunks cost less. Forward chunks are the same sizes in reverse order.
+    of the angles) and the others grow geometrically away from it (by
+    PIPELINE_GROWTH_BP or PIPELINE_GROWTH_FP); the farthest chunk also takes
+    what is left. Forward chunks run from the farthest to the exposed one.
     """
+    growth = PIPELINE_GROWTH_FP if forward else PIPELINE_GROWTH_BP
     sizes, left, size = [], nang, max(1, nang // 32)
     while left > 0:
         sizes.append(min(size, left))
         left -= sizes[-1]
-        size *= PIPELINE_GROWTH
+        size *= growth
+    if len(sizes) > 1 and sizes[-1] < sizes[-2]:
+        rest = sizes.pop()  # a remainder smaller than its neighbour joins it
+        sizes[-1] += rest
     if forward:
         sizes.reverse()
     return np.concatenate([[0], np.cumsum(sizes)]).astype(int)
