@@ -417,6 +417,76 @@ def bench_general_bp(torch, ts, device, steps, n=256, angles=360, det=(256, 384)
             "per_voxel_kernel_equal": same}
 
 
+def bench_fdk(torch, ts, device, x, y, steps):
+    """FDK reconstruction (tomosipo's ``fdk``: cosine weights, ramp filter on the
+    device FFT, bilinear backprojection with FDK weights) of the headline scan's
+    sinogram ``y`` of phantom ``x`` (512^3, 1024 angles over 2 pi, 512 x 768)."""
+    from tomosipo_gb300.fdk import fdk_backproject, fdk_constants, fdk_filter
+    from tomosipo_gb300.projector import create_projector
+
+    vg, pg = workload_geometry(ts)
+    proj = create_projector(vg, pg)
+    w = fdk_constants(vg, pg)[2]
+    out = torch.zeros(tuple(vg.shape), device=device)
+    q = fdk_filter(vg, pg, y)
+    fdk_backproject(proj, out, q, w, False)
+    torch.cuda.synchronize()
+    ev = [[torch.cuda.Event(enable_timing=True) for _ in range(3)] for _ in range(steps)]
+    for e in ev:
+        e[0].record()
+        q = fdk_filter(vg, pg, y)
+        e[1].record()
+        fdk_backproject(proj, out, q, w, False)
+        e[2].record()
+    torch.cuda.synchronize()
+    filt = statistics.mean(e[0].elapsed_time(e[1]) for e in ev)
+    bp = statistics.mean(e[1].elapsed_time(e[2]) for e in ev)
+    U = N ** 3 * ANGLES
+    # reconstruction error on the central half cube (cone-beam FDK is exact on
+    # the central plane only; the phantom's ellipsoids span the volume)
+    c = slice(N // 4, 3 * N // 4)
+    err = float(torch.linalg.vector_norm(out[c, c, c] - x[c, c, c]) / torch.linalg.vector_norm(x[c, c, c]))
+    return {"config": f"FDK of the {N}^3 / {ANGLES}-angle / {DET[0]}x{DET[1]} cone scan "
+                      "(full circle), sinogram in HBM",
+            "ms": filt + bp, "filter_ms": filt, "backprojection_ms": bp,
+            "backprojection_gups": U / (bp / 1e3) / 1e9,
+            "rel_error_central_half_cube": err}
+
+
+def bench_supersampling(torch, ts, device, steps, n=256, angles=360, det=(256, 384), d=2):
+    """Detector supersampling d: FP averages d x d rays per pixel and the matched
+    BP is its exact transpose (both on the d-times finer detector), against the
+    same operator without supersampling. Cone n^3, ``angles`` angles, ``det``."""
+    vg = ts.volume(shape=n, size=1)
+    pg = ts.cone(angles=angles, shape=det, size=np.sqrt(2), cone_angle=0.5)
+    x = phantom_gpu(torch, device, n, count=8, seed=7)
+    out = {}
+    for ss in (1, d):
+        A = ts.operator(vg, pg, detector_supersampling=ss)
+        y = torch.empty(A.range_shape, device=device)
+        v = torch.empty(A.domain_shape, device=device)
+        A(x, out=y)
+        A.T(y, out=v)
+        torch.cuda.synchronize()
+        ev = [[torch.cuda.Event(enable_timing=True) for _ in range(3)] for _ in range(steps)]
+        for e in ev:
+            e[0].record()
+            A(x, out=y)
+            e[1].record()
+            A.T(y, out=v)
+            e[2].record()
+        torch.cuda.synchronize()
+        out[ss] = (statistics.mean(e[0].elapsed_time(e[1]) for e in ev),
+                   statistics.mean(e[1].elapsed_time(e[2]) for e in ev))
+    U = n ** 3 * angles
+    return {"config": f"cone {n}^3, {angles} angles, detector {det[0]}x{det[1]}, "
+                      f"detector_supersampling={d} ({d}x{d} rays per pixel)",
+            "fp_ms": out[d][0], "bp_ms": out[d][1],
+            "plain_fp_ms": out[1][0], "plain_bp_ms": out[1][1],
+            "gups_per_coarse_update": 2 * U / ((out[d][0] + out[d][1]) / 1e3) / 1e9,
+            "gups_per_fine_update": 2 * U * d * d / ((out[d][0] + out[d][1]) / 1e3) / 1e9}
+
+
 def helical_cone_vec(ts, n, angles, rows, cols, rng, jitter_voxels=0.5):
     """Helical cone_vec around z for an n^3 unit-cube volume: source/detector at
     2 sqrt2 from the axis (the detector through it), detector sqrt2 x sqrt2*cols/rows
@@ -776,10 +846,12 @@ def run_ours(args, rank, world, local_rank):
             traffic_source = tj.get("source") if traffic is not None else None
         except (OSError, ValueError):
             traffic = None
-    batched = serving = lpd = bilinear = general = None
+    batched = serving = lpd = bilinear = general = fdk = supersampling = None
     if not args.no_bilinear:
         bilinear = bench_bilinear_pair(torch, ts, device, x, args.steps)
         general = bench_general_bp(torch, ts, device, args.steps)
+        fdk = bench_fdk(torch, ts, device, x, y, min(args.steps, 5))
+        supersampling = bench_supersampling(torch, ts, device, min(args.steps, 5))
     if not args.no_lpd:
         lpd = bench_lpd(torch, ts, device)
     if not args.no_sirt:
@@ -831,6 +903,8 @@ def run_ours(args, rank, world, local_rank):
         "learned_primal_dual": lpd,
         "fp_plus_bilinear_bp": bilinear,
         "tilted_detector_general_bp": general,
+        "fdk": fdk,
+        "detector_supersampling": supersampling,
         "gpu_launches": args.steps * (stats["fp_launches"] + stats["bp_matched_launches"]),
         "clocks": clock_info,
         "plan": stats,
@@ -849,7 +923,9 @@ def main():
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-sirt", action="store_true", help="skip the batched SIRT and serving parts")
     p.add_argument("--no-lpd", action="store_true", help="skip the learned primal-dual step")
-    p.add_argument("--no-bilinear", action="store_true", help="skip the FP + bilinear BP pair")
+    p.add_argument("--no-bilinear", action="store_true",
+                   help="skip the FP + bilinear BP pair, the tilted-detector, FDK and "
+                   "detector-supersampling timings")
     p.add_argument("--sirt-jobs", type=int, default=64)
     p.add_argument("--serve-requests", type=int, default=64)
     p.add_argument("--serve-stable-requests", type=int, default=16)

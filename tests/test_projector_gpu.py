@@ -291,6 +291,10 @@ BP_EDGE_CASES = {
     # (the backprojector's row-loop path)
     "fine_rows": (ts.volume(shape=24, size=1),
                   ts.parallel(angles=12, shape=(80, 36), size=(1.2, 1.5))),
+    # rows 2/3 of a voxel apart: up to four rows per voxel (the voxel-pair
+    # kernel's four-row path; projectors with rows this fine use that kernel)
+    "rows_finer_than_voxels": (ts.volume(shape=24, size=1),
+                               ts.parallel(angles=12, shape=(36, 36), size=(1.0, 1.5))),
     # a detector shorter than the volume: rows clamped into the padding
     "tall_volume": (ts.volume(shape=(150, 20, 36), size=(3.0, 0.4, 0.72)),
                     ts.cone(angles=9, shape=(40, 50), size=(1.2, 1.0), src_orig_dist=3,

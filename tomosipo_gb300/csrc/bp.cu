@@ -120,7 +120,7 @@ __device__ __forceinline__ const float2* row_at(const float2* col, int row, Offs
 // tests once its row index is clamped into the padding. Offsets are 32-bit
 // unless kWide (padded sinogram of 2^31 pairs or more, or rows 2^31 bytes or
 // more apart).
-template <int kA, int kRun, bool kWide>
+template <int kA, int kRun, bool kWide, bool kFine>
 __device__ __forceinline__ void bp_sep_accumulate(const AngleParams* __restrict__ params,
                                                   const ColumnEntry* __restrict__ columns,
                                                   const int* __restrict__ angles, int n_angles,
@@ -218,6 +218,36 @@ __device__ __forceinline__ void bp_sep_accumulate(const AngleParams* __restrict_
             for (int m = 0; m < kA; ++m) acc[m][j] = fmaf(h[m], V, acc[m][j]);
           }
         }
+      } else if (kFine && fabsf(Sl) >= 0.5f) {
+        // (Compiled into the fine-row variant only: the extra path raises the
+        // kernel's register pressure.) Rows finer than voxels, |Sl| in
+        // [0.5, 1) (a detector supersampled twice, for one): the tent of voxel
+        // j (half-width 1/|Sl| <= 2 rows) covers at most four rows, from the
+        // first row above its lower end.
+        // Two row-pair loads read them; each row is weighted by its exact tent
+        // and added in increasing order, as the loop below does, so rows of
+        // weight 0 add nothing. The first row is clamped to [vmin, vmax - 1]
+        // so both pairs lie in the padded sinogram (rows outside the detector
+        // hold zeros; a clamped window still covers the detector rows of the
+        // true one; NaN clamps to vmin).
+        const float2* __restrict__ colv = col + Offset(g.ov) * rs;  // row 0 of this column
+#pragma unroll
+        for (int j = 0; j < kRun; ++j) {
+          const float Bj = B - (zt0 + float(j));
+          float t = fminf((-1.0f - Bj) * inv, (1.0f - Bj) * inv);
+          t = fminf(fmaxf(t, vmin - 1.0f), vmax - 2.0f);
+          const float f = __fadd_rd(t, kFloorMagic);
+          const float v0 = (f - kFloorMagic) + 1.0f;
+          const int r0 = int(__float_as_uint(f) - kFloorBits) + 1;
+          const float2 y01 = __ldg(row_at(colv, r0, rs_bytes));
+          const float2 y23 = __ldg(row_at(colv, r0 + 2, rs_bytes));
+          float V = __saturatef(1.0f - fabsf(fmaf(v0, Sl, Bj))) * y01.x;
+          V = fmaf(__saturatef(1.0f - fabsf(fmaf(v0 + 1.0f, Sl, Bj))), y01.y, V);
+          V = fmaf(__saturatef(1.0f - fabsf(fmaf(v0 + 2.0f, Sl, Bj))), y23.x, V);
+          V = fmaf(__saturatef(1.0f - fabsf(fmaf(v0 + 3.0f, Sl, Bj))), y23.y, V);
+#pragma unroll
+          for (int m = 0; m < kA; ++m) acc[m][j] = fmaf(h[m], V, acc[m][j]);
+        }
       } else {
 #pragma unroll
         for (int j = 0; j < kRun; ++j) {
@@ -256,7 +286,7 @@ enum BpSepMode {
 // registers) measured fastest for 2 x 16 voxels per thread: fewer registers
 // spill the accumulators, more cut occupancy. A block of 128 threads is kTA
 // threads along a times 128 / kTA planes, a-fastest, or plane-fastest (kPF).
-template <int kA, int kRun, bool kWide, bool kAisX, int kTA, bool kPF>
+template <int kA, int kRun, bool kWide, bool kAisX, int kTA, bool kPF, bool kFine = false>
 __device__ __forceinline__ void bp_sep_tile(const AngleParams* __restrict__ params,
                                             const ColumnEntry* __restrict__ columns,
                                             const int* __restrict__ angles, int n_angles,
@@ -282,7 +312,7 @@ __device__ __forceinline__ void bp_sep_tile(const AngleParams* __restrict__ para
   const float kt = kAisX ? yt : xt;
   const float it0 = kAisX ? xt : yt;
   float acc[kA][kRun];
-  bp_sep_accumulate<kA, kRun, kWide>(params, columns, angles, n_angles, sinow, g, kt, it0, z0,
+  bp_sep_accumulate<kA, kRun, kWide, kFine>(params, columns, angles, n_angles, sinow, g, kt, it0, z0,
                                      acc);
 #pragma unroll
   for (int m = 0; m < kA; ++m) {
@@ -307,16 +337,17 @@ __device__ __forceinline__ void bp_sep_tile(const AngleParams* __restrict__ para
   }
 }
 
-template <int kA, int kRun, bool kWide, bool kAisX, int kMode, int kTA, bool kPF>
+// kFine: also the four-row path for detector rows finer than the voxels.
+template <int kA, int kRun, bool kWide, bool kAisX, int kMode, int kTA, bool kPF, bool kFine>
 __global__ void __launch_bounds__(kBpX* kBpY, 6)
     bp_separable_kernel(const AngleParams* __restrict__ params,
                         const ColumnEntry* __restrict__ columns, const int* __restrict__ angles,
                         int n_angles, const float2* __restrict__ sinow, float* __restrict__ vol,
                         DeviceGeometry g, const float* __restrict__ C,
                         float* __restrict__ scratch) {
-  bp_sep_tile<kA, kRun, kWide, kAisX, kTA, kPF>(params, columns, angles, n_angles, sinow, vol, g,
-                                                C, scratch, kMode, blockIdx.x, blockIdx.y,
-                                                blockIdx.z);
+  bp_sep_tile<kA, kRun, kWide, kAisX, kTA, kPF, kFine>(params, columns, angles, n_angles, sinow,
+                                                       vol, g, C, scratch, kMode, blockIdx.x,
+                                                       blockIdx.y, blockIdx.z);
 }
 
 // One SIRT pass of many jobs in one launch: block b runs block b - start[j] of
@@ -708,10 +739,11 @@ __global__ void __launch_bounds__(kGenThreads, 4)
           iv_hi = min(iv_hi, __float2int_ru((vs + dv) + hi_v));
         }
         float acc_m = acc[m];
-        for (int iv = iv_lo; iv <= iv_hi; ++iv) {
-          const int row = (iv - R.v0) * R.sv - R.u0 * R.su;
-          for (int iu = iu_lo; iu <= iu_hi; ++iu) {
-            const int st = row + iu * R.su;
+        // stage index of (iv_lo, iu_lo), region-relative (small), then steps
+        int st_row = (iv_lo - R.v0) * R.sv + (iu_lo - R.u0) * R.su;
+        for (int iv = iv_lo; iv <= iv_hi; ++iv, st_row += R.sv) {
+          int st = st_row;
+          for (int iu = iu_lo; iu <= iu_hi; ++iu, st += R.su) {
             const float4 r4 = s_ray[st];
             // tent(t) as one saturating add (1 - |t| <= 1; NaN saturates to
             // 0); a weight of 0 adds nothing
@@ -1017,11 +1049,22 @@ dim3 sep_grid(const DeviceGeometry& g, bool a_is_x, int ta, bool pf) {
   return dim3(pf ? gp : ga, pf ? ga : gp, (g.nz + kRunZ - 1) / kRunZ);
 }
 
+// Projectors with rows finer than the voxels (fine_rows) take the fine-row
+// variant for plain backprojections with 32-bit offsets; batched SIRT passes
+// and 64-bit offsets keep the general row loop for them.
 template <bool kWide, bool kAisX, int kMode, int kTA, bool kPF>
 void launch_sep_tile(const tsgb_projector* p, const int* angles, int n, const float2* pairs,
                      float* vol, const float* C, float* scratch, cudaStream_t stream) {
   const dim3 grid = sep_grid(p->g, kAisX, kTA, kPF);
-  bp_separable_kernel<kSepA, kRunZ, kWide, kAisX, kMode, kTA, kPF>
+  if constexpr (!kWide && (kMode == kBpSet || kMode == kBpAdd)) {
+    if (p->fine_rows) {
+      bp_separable_kernel<kSepA, kRunZ, kWide, kAisX, kMode, kTA, kPF, true>
+          <<<grid, kBpX * kBpY, 0, stream>>>(p->d_params, p->d_columns, angles, n, pairs, vol,
+                                             p->g, C, scratch);
+      return;
+    }
+  }
+  bp_separable_kernel<kSepA, kRunZ, kWide, kAisX, kMode, kTA, kPF, false>
       <<<grid, kBpX * kBpY, 0, stream>>>(p->d_params, p->d_columns, angles, n, pairs, vol, p->g,
                                          C, scratch);
 }

@@ -173,6 +173,8 @@ std::string build_plan(const tsgb_volume_desc* vol, const tsgb_projection_desc* 
   p->layouts.clear();
   columns->assign(size_t(g.nangles) * g.cols, ColumnEntry{});
   sep_angles->clear();
+  p->fine_rows = false;
+  double fine_planes = 0.0, all_planes = 0.0;  // (separable angle, column, plane) triples
   gen_angles->clear();
   bil_fast->clear();
   bil_slow->clear();
@@ -291,6 +293,25 @@ std::string build_plan(const tsgb_volume_desc* vol, const tsgb_projection_desc* 
       gen_angles->push_back(t);
     else
       sep_angles->push_back(t);
+    // Planes on which a column's rows lie closer than one voxel: the row step
+    // q_b'(vt) = R + kt S is linear in the plane kt, so |R + kt S| < 1 on one
+    // interval of planes; count the planes of [k_lo, k_hi] in it.
+    if (!ap.bp_general) {
+      const double k_lo = -double(anchor[d]), k_hi = double(shape[d] - 1 - anchor[d]);
+      for (int iu = 0; iu < g.cols; ++iu) {
+        const ColumnEntry& c = (*columns)[size_t(t) * g.cols + iu];
+        double lo = k_lo, hi = k_hi;
+        if (c.S != 0.0f) {
+          const double a = (-1.0 - double(c.R)) / double(c.S), b = (1.0 - double(c.R)) / double(c.S);
+          lo = std::max(lo, std::floor(std::min(a, b)) + 1.0);
+          hi = std::min(hi, std::ceil(std::max(a, b)) - 1.0);
+        } else if (!(std::fabs(double(c.R)) < 1.0)) {
+          hi = lo - 1.0;
+        }
+        if (hi >= lo) fine_planes += hi - lo + 1.0;
+        all_planes += k_hi - k_lo + 1.0;
+      }
+    }
   }
 
   int64_t off = 0;
@@ -314,6 +335,10 @@ std::string build_plan(const tsgb_volume_desc* vol, const tsgb_projection_desc* 
     ap.vs_b = float(vs[L.b]);
   }
   p->fp_workspace_elems = off;
+  // Most of the separable work on rows finer than the voxels (a supersampled
+  // or fine detector; about 0.6 % of it for the cone scans of the benchmark):
+  // the matched backprojection takes the voxel-pair kernel's fine-row variant.
+  p->fine_rows = all_planes > 0.0 && fine_planes >= 0.25 * all_planes;
   p->n_general_bp = int(gen_angles->size());
   // Separable angles grouped by their in-plane axis a (x first, then y): the
   // backprojector runs one pass per group, each with voxel runs along a.

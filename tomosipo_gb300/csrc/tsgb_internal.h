@@ -119,6 +119,11 @@ struct tsgb_projector {
   int n_general_bp = 0;         // angles handled by the general BP kernel
   int n_separable_bp = 0;       // angles handled by the separable BP kernel
   int n_sep_ax = 0;             // of those, the first n_sep_ax have a = x (the rest a = y)
+  // On at least a quarter of the (separable angle, column, plane) triples the
+  // detector rows lie closer than one voxel apart (|q_b step per row| < 1):
+  // the matched backprojection then runs the voxel-pair kernel's fine-row
+  // variant.
+  bool fine_rows = false;
   int n_bil_fast = 0;           // bilinear BP: angles for the z-flat kernel
   int n_bil_slow = 0;           // bilinear BP: angles for the general kernel
   tsgb::AngleParams* d_params = nullptr;
@@ -246,11 +251,14 @@ int launch_bp_sep_multi(const BpMulti& m, bool a_is_x, void* stream);
 
 // The matched backprojector of det_v-along-z angles is the z-lane kernel
 // (bp_zlane.cu, column-major weighted sinogram) unless the tuning picks the
-// voxel-pair kernel (bp.cu, row-major) or the volume's (y, x) plane is too
+// voxel-pair kernel (bp.cu, row-major), the volume's (y, x) plane is too
 // large for the z-lane grid (fewer than 2^32 voxel columns keep it below 2^31
-// blocks for every shape, which hold at least 8 columns per block).
+// blocks for every shape, which hold at least 8 columns per block), or the
+// detector rows are mostly finer than the voxels (fine_rows: the voxel-pair
+// kernel has a fast path for that).
 inline bool bp_uses_zlane(const tsgb_projector* p) {
-  return p->tuning.bp_kernel == 1 && int64_t(p->g.nx) * p->g.ny < (int64_t(1) << 32);
+  return p->tuning.bp_kernel == 1 && !p->fine_rows &&
+         int64_t(p->g.nx) * p->g.ny < (int64_t(1) << 32);
 }
 inline int zlane_shape(const tsgb_projector* p) { return p->tuning.bp_shape; }
 
