@@ -7,7 +7,7 @@ import torch
 
 import tomosipo_gb300 as ts
 from oracle import fdk_oracle
-from tests.helpers import rel_l2
+from tests.helpers import helical_cone_vec, rel_l2
 from tomosipo_gb300 import fdk
 
 
@@ -20,13 +20,18 @@ def _scans():
     circular = ts.cone(angles=17, **kw)
     lift = np.stack([np.linspace(-0.2, 0.2, 17), np.zeros(17), np.zeros(17)], axis=1)
     rot = ts.rotate(pos=0, axis=(1.0, 0.4, -0.3), angles=0.5)
+    # per-angle source and detector jitter: the cosine weights differ per angle
+    # (the other scans share one weight map)
+    jittered = helical_cone_vec(17, (9, 13), (1.2, 1.6), 3.0, 1.5, pitch=0.0, jitter=0.5,
+                                voxel=0.05)
     return {"circular": circular, "helical": ts.translate(lift) * circular.to_vec(),
             "rotated": rot * circular.to_vec(), "short": ts.cone(angles=SHORT, **kw),
-            "short_rotated_reversed": rot * ts.cone(angles=-SHORT, **kw).to_vec()}
+            "short_rotated_reversed": rot * ts.cone(angles=-SHORT, **kw).to_vec(),
+            "jittered": jittered}
 
 
 @pytest.mark.parametrize("scan", ["circular", "helical", "rotated", "short",
-                                  "short_rotated_reversed"])
+                                  "short_rotated_reversed", "jittered"])
 def test_filter_and_angle_weights_match_the_oracle(scan):
     pg = _scans()[scan]
     short = scan.startswith("short")
@@ -83,10 +88,27 @@ def test_ramp_spectrum_is_the_zero_padded_ram_lak_kernel():
     is the kernel's sum, 1/4 - 2 sum_{odd n < cols} 1/(pi n)^2 (small and
     positive), and it rises to about |f| = 1/2 at the Nyquist frequency."""
     spec, length = fdk.ramp_spectrum(13, "cpu")
-    assert length == 32 and spec.shape == (17,)
+    assert length == fdk.fft_length(13) == 28 and spec.shape == (15,)
     odd = np.arange(1, 13, 2)
     assert spec[0].item() == pytest.approx(0.25 - 2 * np.sum(1 / (np.pi * odd) ** 2), abs=1e-6)
     assert torch.all(spec[1:] > spec[:-1]) and spec[-1].item() == pytest.approx(0.5, abs=0.01)
+
+
+@pytest.mark.parametrize("cols", [1, 9, 13, 192, 384, 768, 1000, 1021])
+def test_fft_length_avoids_wrap_around_with_fast_radices(cols):
+    """The filter's FFT length holds a linear convolution of a row with the
+    kernel's 2 cols - 1 taps, is even, and has only the prime factors 2, 3, 5
+    and 7; it is the smallest such length."""
+    n = fdk.fft_length(cols)
+
+    def smooth(m):
+        for f in (2, 3, 5, 7):
+            while m % f == 0:
+                m //= f
+        return m == 1
+
+    assert n >= 2 * cols - 1 and n % 2 == 0 and smooth(n)
+    assert not any(smooth(m) and m % 2 == 0 for m in range(max(2 * cols - 1, 2), n))
 
 
 def test_fdk_rejects_parallel_beams():

@@ -149,9 +149,25 @@ def short_scan_weights(vg, pg):
     return 2 * parker_weights(rel[:, None], gamma, delta)
 
 
+def fft_length(cols):
+    """Smallest length >= 2 cols - 1 (a linear convolution of a row with the
+    kernel's 2 cols - 1 taps, without wrap-around) whose prime factors are 2,
+    3, 5 and 7 (fast FFT radices): 1536 for 768 columns, where the next power
+    of two would be 2048."""
+    n = max(2 * cols - 1, 2)
+    while True:
+        m = n
+        for f in (2, 3, 5, 7):
+            while m % f == 0:
+                m //= f
+        if m == 1 and n % 2 == 0:
+            return n
+        n += 1
+
+
 def ramp_spectrum(cols, device):
-    """Real spectrum of the unit-pitch Ram-Lak kernel, zero-padded to >= 2 cols."""
-    length = 1 << int(math.ceil(math.log2(max(2 * cols, 2))))
+    """Real spectrum of the unit-pitch Ram-Lak kernel, zero-padded to fft_length(cols)."""
+    length = fft_length(cols)
     g = np.zeros(length)
     g[0] = 0.25
     odd = np.arange(1, cols, 2)
@@ -160,11 +176,14 @@ def ramp_spectrum(cols, device):
     return torch.from_numpy(np.fft.rfft(g).real.astype(np.float32)).to(device), length
 
 
-def fdk_filter(vg, pg, y, angle_chunk=64, short_scan=False):
+def fdk_filter(vg, pg, y, angle_chunk=None, short_scan=False):
     """Cosine-weighted (and with ``short_scan`` Parker-weighted), ramp-filtered
-    copy of sinogram ``y`` (a CUDA tensor)."""
+    copy of sinogram ``y`` (a CUDA tensor). Angles are filtered ``angle_chunk``
+    at a time (default: as many as fit a 512 MB zero-padded buffer)."""
     rows, nang, cols = y.shape
     dev = y.device
+    if angle_chunk is None:
+        angle_chunk = max(1, (512 << 20) // (rows * fft_length(cols) * 4))
     sdd, pitch, _ = fdk_constants(vg, pg)
     S, D, U, V = _vectors(pg)
     parker = (torch.from_numpy(short_scan_weights(vg, pg).astype(np.float32)).to(dev)
@@ -176,23 +195,41 @@ def fdk_filter(vg, pg, y, angle_chunk=64, short_scan=False):
         2 * np.einsum("ij,ij->i", w0, V), 2 * np.einsum("ij,ij->i", w0, U),
         2 * np.einsum("ij,ij->i", U, V), sdd, 1.0 / pitch,
     ], axis=1)
+    # A circular scan (the detector turning with the source) has the same
+    # cosine-weight coefficients (the first 7) at every angle: one weight map
+    # then serves all angles. (Compared relative to the largest: some are zero
+    # up to rounding. The last, 1 / pitch, can vary: the pitch is referred to
+    # the anchor voxel, off the rotation axis by half a voxel in an even-sized
+    # volume; it is applied per angle either way.)
+    cw = per_angle[:, :7]
+    same = bool(np.all(np.abs(cw - cw[:1]) <= 1e-12 * np.abs(cw).max()))
     c = torch.from_numpy(per_angle).to(dev)
     a = torch.arange(rows, device=dev, dtype=torch.float64) + 0.5 - rows / 2
     b = torch.arange(cols, device=dev, dtype=torch.float64) + 0.5 - cols / 2
-    spec, length = ramp_spectrum(cols, dev)
-    q = torch.empty_like(y, dtype=torch.float32)
-    for t0 in range(0, nang, angle_chunk):
-        t1 = min(nang, t0 + angle_chunk)
-        k = c[t0:t1]
+
+    def cosine_weights(k):
         A, B = a[:, None, None], b[None, None, :]
         dist2 = (k[None, :, 0, None] + A * A * k[None, :, 1, None] + B * B * k[None, :, 2, None]
                  + A * k[None, :, 3, None] + B * k[None, :, 4, None] + A * B * k[None, :, 5, None])
-        cosw = (k[None, :, 6, None] / torch.sqrt(dist2)).to(torch.float32)
-        p = y[:, t0:t1, :].to(torch.float32) * cosw
+        return (k[None, :, 6, None] / torch.sqrt(dist2)).to(torch.float32)
+
+    shared = cosine_weights(c[:1]) if same else None
+    spec, length = ramp_spectrum(cols, dev)
+    q = torch.empty_like(y, dtype=torch.float32)
+    buf = None  # weighted rows, zero-padded to the FFT length (the padding stays zero)
+    for t0 in range(0, nang, angle_chunk):
+        t1 = min(nang, t0 + angle_chunk)
+        if buf is None or buf.shape[1] != t1 - t0:
+            buf = torch.zeros((rows, t1 - t0, length), dtype=torch.float32, device=dev)
+        k = c[t0:t1]
+        w = shared if same else cosine_weights(k)
         if parker is not None:
-            p = p * parker[None, t0:t1, :]
-        f = torch.fft.irfft(torch.fft.rfft(p, n=length, dim=-1) * spec, n=length, dim=-1)[..., :cols]
-        q[:, t0:t1, :] = f * k[None, :, 7, None].to(torch.float32)
+            w = w * parker[None, t0:t1, :]
+        torch.mul(y[:, t0:t1, :].to(torch.float32), w, out=buf[..., :cols])
+        f = torch.fft.rfft(buf, dim=-1)
+        # the ramp times each angle's 1 / pitch, in one pass over the spectrum
+        f.mul_(spec * k[None, :, 7, None].to(torch.float32))
+        q[:, t0:t1, :] = torch.fft.irfft(f, n=length, dim=-1)[..., :cols]
     return q
 
 
