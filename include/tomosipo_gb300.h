@@ -106,8 +106,14 @@ int tsgb_direct_fp_batch(tsgb_projector* p, const float* vol, float* sino, int64
                          void* stream);
 
 /* Backprojection of n sinograms into n volumes, laid out as for
- * tsgb_direct_fp_batch, each as tsgb_direct_bp. Replaces the per-slice loop
- * of to_autograd's backward pass (tomosipo/torch_support.py:70-74). */
+ * tsgb_direct_fp_batch, each as tsgb_direct_bp (equal results). Replaces the
+ * per-slice loop of to_autograd's backward pass
+ * (tomosipo/torch_support.py:70-74). With a workspace of
+ * tsgb_bp_batch_workspace_bytes(p, n, bp_kind) bytes, matched
+ * backprojections of the voxel-pair kernel run on multi-job launches (one
+ * launch per pass over up to 48 items, which fill the GPU where one small
+ * volume does not); with tsgb_bp_workspace_bytes, one item after another. */
+int64_t tsgb_bp_batch_workspace_bytes(const tsgb_projector* p, int64_t n, int32_t bp_kind);
 int tsgb_direct_bp_batch(tsgb_projector* p, float* vol, const float* sino, int64_t n,
                          int32_t additive, int32_t bp_kind, void* workspace,
                          int64_t workspace_bytes, void* stream);

@@ -182,3 +182,35 @@ def test_batched_extra_dims_equal_per_slice(dev):
         fb = to_autograd(A.T, num_extra_dims=1)
         yy = torch.rand(4, *A.range_shape, device=dev)
         assert torch.equal(fb(yy), torch.stack([A.T(yy[i]) for i in range(4)]))
+
+
+def test_batched_backprojection_in_groups_equals_per_item(dev):
+    """A batched matched backprojection of the voxel-pair kernel runs on
+    multi-job launches (one per pass over up to 48 items) when given the batch
+    workspace: 50 items (two groups) equal backprojecting each on its own, bit
+    for bit, setting and adding."""
+    from tomosipo_gb300 import _native
+
+    vg = ts.volume(shape=(16, 18, 20), size=1)
+    pg = ts.cone(angles=9, shape=(16, 24), size=(1.2, 1.5), cone_angle=0.4)
+    A = ts.operator(vg, pg)
+    A.projector.set_tuning(dev.index, bp_kernel=0)
+    lib = _native.load()
+    h = A.projector.handle(dev.index)
+    one = lib.tsgb_bp_workspace_bytes(h, 0)
+    assert lib.tsgb_bp_batch_workspace_bytes(h, 50, 0) > one
+    assert lib.tsgb_bp_batch_workspace_bytes(h, 1, 0) == one
+    n = 50
+    yy = torch.rand(n, *A.range_shape, device=dev)
+    out = torch.full((n, *A.domain_shape), 7.0, device=dev)
+    A.T._apply_batch(yy, out)
+    ref = torch.stack([A.T(yy[i]) for i in range(n)])
+    assert torch.equal(out, ref)
+    B = ts.operator(vg, pg, additive=True)
+    B.projector.set_tuning(dev.index, bp_kernel=0)
+    acc = ref.clone()
+    B.T._apply_batch(yy, acc)
+    ref_add = ref.clone()
+    for i in range(n):
+        B.T(yy[i], out=ref_add[i])
+    assert torch.equal(acc, ref_add)

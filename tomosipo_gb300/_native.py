@@ -72,6 +72,8 @@ SIGNATURES = {
     "tsgb_projector_destroy": (ctypes.c_int, [ctypes.c_void_p]),
     "tsgb_fp_workspace_bytes": (ctypes.c_int64, [ctypes.c_void_p]),
     "tsgb_bp_workspace_bytes": (ctypes.c_int64, [ctypes.c_void_p, ctypes.c_int32]),
+    "tsgb_bp_batch_workspace_bytes": (ctypes.c_int64, [ctypes.c_void_p, ctypes.c_int64,
+                                                       ctypes.c_int32]),
     "tsgb_direct_fp": (
         ctypes.c_int,
         [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int32, ctypes.c_void_p,

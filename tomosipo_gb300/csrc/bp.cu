@@ -1132,6 +1132,27 @@ void launch_sep_pass(const tsgb_projector* p, bool a_is_x, const int* angles, in
     launch_sep_pass_m<false, false>(p, angles, n, mode, pairs, vol, C, scratch, stream);
 }
 
+// Row-major row-pair weighted sinogram of angles [angle_begin, angle_end)
+// into `pairs` (bp_weight_kernel), and the padding rows it does not write
+// zeroed: -kRowPad .. -2 and rows .. rows + kRowPad - 1.
+void launch_bp_weight_rows(const tsgb_projector* p, const float* sino, float2* pairs,
+                           int angle_begin, int angle_end, cudaStream_t stream) {
+  const DeviceGeometry& g = p->g;
+  const size_t rs = (size_t)g.nangles * g.cols;  // elements between rows
+  const dim3 block(32, 8);
+  for (int a0 = angle_begin; a0 < angle_end; a0 += 65535) {
+    const int n = angle_end - a0 < 65535 ? angle_end - a0 : 65535;
+    const dim3 grid((g.cols + 31) / 32, (g.rows + 1 + 8 * kWeightRows - 1) / (8 * kWeightRows),
+                    n);
+    // offset the angle through the pointers: rows are strided by nangles*cols
+    bp_weight_kernel<<<grid, block, 0, stream>>>(p->d_params + a0, p->d_columns + (size_t)a0 * g.cols,
+                                                 sino + (size_t)a0 * g.cols,
+                                                 pairs + kRowPad * rs + (size_t)a0 * g.cols, g);
+  }
+  cudaMemsetAsync(pairs, 0, (kRowPad - 1) * rs * sizeof(float2), stream);
+  cudaMemsetAsync(pairs + (kRowPad + g.rows) * rs, 0, kRowPad * rs * sizeof(float2), stream);
+}
+
 // Entries of host_list[lo, hi) (angle ids in increasing order) that lie in
 // [a0, a1): offset into the list and count.
 void angle_sub_range(const std::vector<int>& host_list, int lo, int hi, int a0, int a1, int& off,
@@ -1169,23 +1190,7 @@ int launch_bp_matched(const tsgb_projector* p, float* vol, const float* sino, bo
                         stream);
     return int(cudaGetLastError());
   }
-  const size_t rs = (size_t)g.nangles * g.cols;  // elements between rows
-  {
-    const dim3 block(32, 8);
-    for (int a0 = angle_begin; a0 < angle_end; a0 += 65535) {
-      const int n = angle_end - a0 < 65535 ? angle_end - a0 : 65535;
-      const dim3 grid((g.cols + 31) / 32, (g.rows + 1 + 8 * kWeightRows - 1) / (8 * kWeightRows),
-                      n);
-      // offset the angle through the pointers: rows are strided by nangles*cols
-      bp_weight_kernel<<<grid, block, 0, stream>>>(p->d_params + a0, p->d_columns + (size_t)a0 * g.cols,
-                                                   sino + (size_t)a0 * g.cols,
-                                                   pairs + kRowPad * rs + (size_t)a0 * g.cols, g);
-    }
-  }
-  // zero the padding rows the weight pass does not write: -kRowPad .. -2 and
-  // rows .. rows + kRowPad - 1
-  cudaMemsetAsync(pairs, 0, (kRowPad - 1) * rs * sizeof(float2), stream);
-  cudaMemsetAsync(pairs + (kRowPad + g.rows) * rs, 0, kRowPad * rs * sizeof(float2), stream);
+  launch_bp_weight_rows(p, sino, pairs, angle_begin, angle_end, stream);
   if (n_ax > 0)
     launch_sep_pass(p, true, p->d_sep_angles + off_x, n_ax, additive ? kBpAdd : kBpSet, pairs,
                     vol, nullptr, nullptr, stream);
@@ -1283,6 +1288,54 @@ int launch_bp_sep_multi(const BpMulti& m, bool a_is_x, void* stream_) {
   else
     bp_separable_multi_kernel<kSepA, kRunZ, false, kTileAy, kPlaneFastAy>
         <<<unsigned(blocks), kBpX * kBpY, 0, stream>>>(m);
+  return int(cudaGetLastError());
+}
+
+bool bp_batch_multi_eligible(const tsgb_projector* p) {
+  int gx = 0, gy = 0;
+  return !p->fine && !bp_uses_zlane(p) && !p->fine_rows && p->n_general_bp == 0 &&
+         p->n_separable_bp > 0 && bp_sep_blocks(p, true, &gx, &gy) >= 0 &&
+         bp_sep_blocks(p, false, &gx, &gy) >= 0;
+}
+
+int launch_bp_matched_batch(const tsgb_projector* p, float* vol, const float* sino, int64_t n,
+                            bool additive, char* workspace, int64_t item_bytes, void* stream_) {
+  cudaStream_t stream = static_cast<cudaStream_t>(stream_);
+  const DeviceGeometry& g = p->g;
+  const size_t vol_elems = size_t(g.nz) * g.ny * g.nx;
+  const size_t sino_elems = size_t(g.rows) * g.nangles * g.cols;
+  const int n_ax = p->n_sep_ax, n_ay = p->n_separable_bp - p->n_sep_ax;
+  for (int64_t i0 = 0; i0 < n; i0 += kMaxMultiJobs) {
+    const int m = int(std::min<int64_t>(kMaxMultiJobs, n - i0));
+    for (int k = 0; k < m; ++k)
+      launch_bp_weight_rows(p, sino + (i0 + k) * sino_elems,
+                            reinterpret_cast<float2*>(workspace + k * item_bytes), 0, g.nangles,
+                            stream);
+    // the pass along x sets (or adds), the pass along y adds onto it
+    for (int pass = 0; pass < 2; ++pass) {
+      const bool a_is_x = pass == 0;
+      const int n_pass = a_is_x ? n_ax : n_ay;
+      if (n_pass == 0) continue;
+      BpMulti bm{};
+      for (int k = 0; k < m; ++k) {
+        BpMultiJob& J = bm.job[k];
+        J.params = p->d_params;
+        J.columns = p->d_columns;
+        J.angles = p->d_sep_angles + (a_is_x ? 0 : n_ax);
+        J.n_angles = n_pass;
+        J.pairs = reinterpret_cast<const float*>(workspace + k * item_bytes);
+        J.vol = vol + (i0 + k) * vol_elems;
+        J.C = nullptr;
+        J.scratch = nullptr;
+        J.mode = (additive || (!a_is_x && n_ax > 0)) ? kBpAdd : kBpSet;
+        J.g = g;
+        bm.start[k + 1] = bm.start[k] + bp_sep_blocks(p, a_is_x, &J.gx, &J.gy);
+      }
+      bm.n = m;
+      const int rc = launch_bp_sep_multi(bm, a_is_x, stream);
+      if (rc != 0) return rc;
+    }
+  }
   return int(cudaGetLastError());
 }
 

@@ -1,6 +1,8 @@
 // extern "C" entry points of libtomosipo_gb300 (declared in include/tomosipo_gb300.h).
 #include <cuda_runtime.h>
 
+#include <algorithm>
+
 #include <cstdio>
 #include <cstring>
 #include <new>
@@ -266,6 +268,14 @@ int tsgb_direct_fp_batch(tsgb_projector* p, const float* vol, float* sino, int64
   return TSGB_OK;
 }
 
+int64_t tsgb_bp_batch_workspace_bytes(const tsgb_projector* p, int64_t n, int32_t bp_kind) {
+  const int64_t one = tsgb_bp_workspace_bytes(p, bp_kind);
+  if (one < 0 || n <= 1 || bp_kind != TSGB_BP_MATCHED || !tsgb::bp_batch_multi_eligible(p))
+    return one;
+  return std::max<int64_t>(one, std::min<int64_t>(n, tsgb::kMaxMultiJobs) *
+                                    tsgb::bp_pairs_bytes(p->g));
+}
+
 int tsgb_direct_bp_batch(tsgb_projector* p, float* vol, const float* sino, int64_t n,
                          int32_t additive, int32_t bp_kind, void* workspace,
                          int64_t workspace_bytes, void* stream) {
@@ -273,6 +283,18 @@ int tsgb_direct_bp_batch(tsgb_projector* p, float* vol, const float* sino, int64
   if (!p || !vol || !sino || n < 0) return fail(TSGB_ERR_INVALID, "NULL projector or data pointer");
   const size_t vol_elems = size_t(p->g.nz) * p->g.ny * p->g.nx;
   const size_t sino_elems = size_t(p->g.rows) * p->g.nangles * p->g.cols;
+  // multi-job launches when the workspace holds a weighted sinogram per item
+  // of a group (tsgb_bp_batch_workspace_bytes); else one item after another
+  if (n > 1 && bp_kind == TSGB_BP_MATCHED && tsgb::bp_batch_multi_eligible(p) && workspace &&
+      workspace_bytes >= tsgb_bp_batch_workspace_bytes(p, n, bp_kind)) {
+    int rc = check_device(p);
+    if (rc != TSGB_OK) return rc;
+    cudaError_t e = cudaError_t(tsgb::launch_bp_matched_batch(
+        p, vol, sino, n, additive != 0, static_cast<char*>(workspace), tsgb::bp_pairs_bytes(p->g),
+        stream));
+    if (e != cudaSuccess) return cuda_fail(e, "batched backprojection launch");
+    return TSGB_OK;
+  }
   for (int64_t i = 0; i < n; ++i) {
     const int rc = tsgb_direct_bp(p, vol + i * vol_elems, sino + i * sino_elems, additive, bp_kind,
                                   workspace, workspace_bytes, stream);

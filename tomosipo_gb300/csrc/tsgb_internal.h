@@ -248,6 +248,14 @@ int launch_fp_multi(const FpMulti& m, bool pair_layout, void* stream);
 // the multi-job launch of that pass over several jobs (bp.cu).
 long long bp_sep_blocks(const tsgb_projector* p, bool a_is_x, int* gx, int* gy);
 int launch_bp_sep_multi(const BpMulti& m, bool a_is_x, void* stream);
+// Whether a projector's batched matched backprojection can run on multi-job
+// launches (voxel-pair kernel, separable angles only, 32-bit offsets, no
+// supersampling or fine-row variant), and that batched backprojection:
+// n items, item k's weighted sinogram at workspace + (k % kMaxMultiJobs) *
+// item_bytes (item_bytes >= bp_pairs_bytes), in groups of kMaxMultiJobs (bp.cu).
+bool bp_batch_multi_eligible(const tsgb_projector* p);
+int launch_bp_matched_batch(const tsgb_projector* p, float* vol, const float* sino, int64_t n,
+                            bool additive, char* workspace, int64_t item_bytes, void* stream);
 
 // The matched backprojector of det_v-along-z angles is the z-lane kernel
 // (bp_zlane.cu, column-major weighted sinogram) unless the tuning picks the
