@@ -935,11 +935,26 @@ __device__ __forceinline__ float bilinear_z_term(const float4* __restrict__ colq
                                                  float vt,
                                                  float vmin, float vmax, bool clamp, float fu,
                                                  float K, float dz, float dxy2, float acc) {
-  float fv0 = floorf(vt);
-  const float fv = vt - fv0;
-  if (clamp) fv0 = fminf(fmaxf(fv0, vmin), vmax);  // rows outside read the zero padding
+  float fv;
+  int row;
+  if constexpr (kCone) {
+    // Row floor(vt) by kFloorMagic (no conversion unit: the cone weight's
+    // rsqrt shares it). Clamping vt to the integers [vmin, vmax] clamps its
+    // floor: rows outside read the zero padding (their fraction multiplies
+    // zeros; NaN clamps to vmin). Measured 142.6 -> 140.4 ms at 512^3 / 1024;
+    // the FDK-weighted variant measured slower with it, so keeps floorf.
+    const float t = clamp ? fminf(fmaxf(vt, vmin), vmax) : vt;
+    const float f = __fadd_rd(t, kFloorMagic);
+    fv = t - (f - kFloorMagic);
+    row = int(__float_as_uint(f) - kFloorBits);
+  } else {
+    float fv0 = floorf(vt);
+    fv = vt - fv0;
+    if (clamp) fv0 = fminf(fmaxf(fv0, vmin), vmax);  // rows outside read the zero padding
+    row = (int)fv0;
+  }
   const float4 q = __ldg(reinterpret_cast<const float4*>(reinterpret_cast<const char*>(colq) +
-                                                       (long long)(int)fv0 * rs_bytes));
+                                                       (long long)row * rs_bytes));
   const float top = fmaf(fu, q.y - q.x, q.x);
   const float bot = fmaf(fu, q.w - q.z, q.z);
   const float val = fmaf(fv, bot - top, top);
