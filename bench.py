@@ -784,6 +784,23 @@ def run_ours(args, rank, world, local_rank):
             A(xh, out=yh)
             A.T(yh, out=vh)
         torch.cuda.synchronize()
+        # the host's own copy rate just before the timed leg: one plain upload
+        # and download of the volume buffer (0.54 GB each), so a slow end-to-end
+        # number can be told apart from a pipeline that fails to hide copies
+        xd = torch.empty_like(x)
+        cev = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
+        cev[0].record(stream)
+        xd.copy_(xh, non_blocking=True)
+        cev[1].record(stream)
+        vh.copy_(xd, non_blocking=True)
+        cev[2].record(stream)
+        torch.cuda.synchronize()
+        vol_gb = 4 * N ** 3 / 1e9
+        copy_rate = {"h2d_gbs": round(vol_gb / (cev[0].elapsed_time(cev[1]) / 1e3), 1),
+                     "d2h_gbs": round(vol_gb / (cev[1].elapsed_time(cev[2]) / 1e3), 1),
+                     "what": "one plain copy of the volume buffer each way before the timed leg "
+                             "(full rate on this host type: about 210 up, 192 down)"}
+        del xd
         barrier()
         from tomosipo_gb300.projector import TransferTimeline, record_transfers
 
@@ -817,6 +834,7 @@ def run_ours(args, rank, world, local_rank):
             "fp_ms": 1e3 * statistics.median(c[0] for c in calls),
             "bp_ms": 1e3 * statistics.median(c[1] for c in calls),
             "per_step_device_ms": breakdown,
+            "host_copy_rate": copy_rate,
             "path": "ts.operator A(x_host)->y_host, A.T(y_host)->x_host, page-locked huge-page host buffers (ts.host_buffer)",
         }
 
