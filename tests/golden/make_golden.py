@@ -5,8 +5,10 @@
 The reference has no golden FP/BP vectors of its own (its operator tests are
 relational), so these fixtures pin the oracle's outputs on small seeded cases:
 tests check the oracle against them (regression) and the GPU kernels against
-them (parity without rerunning the oracle). ``reference_pins.json`` holds the
-one numeric output the reference publishes for this path.
+them (parity without rerunning the oracle). ``reference_pins.json`` (not
+written by this script) holds outputs the reference's notebooks print: the one
+numeric projection output it publishes for this path, and the reprs of its
+unit cone geometry.
 """
 import json
 import os

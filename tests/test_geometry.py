@@ -181,3 +181,18 @@ def test_hollow_box_phantom_mean():
     vd = ts.data(ts.volume(shape=100))
     ts.phantom.hollow_box(vd)
     assert vd.data.mean() == pytest.approx(0.208)
+
+
+def test_reference_notebook_unit_cone_repr():
+    """The reference's getting-started notebook prints the unit cone of the
+    benchmark's geometry family and the default volume
+    (``notebooks/00_getting_started_google_colab.ipynb`` cell 1): cone_angle
+    0.5 with a sqrt(2) detector puts source and detector 2 sqrt(2) from the
+    origin. The reprs here are the same text."""
+    import json
+    import os
+
+    with open(os.path.join(os.path.dirname(__file__), "golden", "reference_pins.json")) as f:
+        pin = json.load(f)["colab_notebook_unit_cone_repr"]
+    assert repr(ts.cone(angles=20, size=np.sqrt(2), cone_angle=0.5)) == pin["cone_repr"]
+    assert repr(ts.volume()) == pin["volume_repr"]
