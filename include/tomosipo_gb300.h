@@ -97,10 +97,13 @@ int tsgb_direct_bp(tsgb_projector* p, float* vol, const float* sino,
 
 /* Forward projection of n volumes stored back to back (item i at
  * vol + i * Nz*Ny*Nx) into n sinograms (sino + i * rows*num_angles*cols), each
- * as tsgb_direct_fp, in one call; one workspace of tsgb_fp_workspace_bytes
- * serves every item (the projections run one after another on ``stream``).
- * Replaces the per-slice loop over batch and channel dimensions of tomosipo's
- * to_autograd (tomosipo/torch_support.py:49-53). */
+ * as tsgb_direct_fp (equal results), in one call. Replaces the per-slice loop
+ * over batch and channel dimensions of tomosipo's to_autograd
+ * (tomosipo/torch_support.py:49-53). With a workspace of
+ * tsgb_fp_batch_workspace_bytes(p, n) bytes (volume copies per item), the
+ * items run on multi-job launches (one ray launch over up to 48 items); with
+ * tsgb_fp_workspace_bytes, one after another on ``stream``. */
+int64_t tsgb_fp_batch_workspace_bytes(const tsgb_projector* p, int64_t n);
 int tsgb_direct_fp_batch(tsgb_projector* p, const float* vol, float* sino, int64_t n,
                          int32_t additive, void* workspace, int64_t workspace_bytes,
                          void* stream);

@@ -126,6 +126,7 @@ _NULL_CALLS = {
     "tsgb_fp_workspace_bytes": (None,),
     "tsgb_bp_workspace_bytes": (None, 0),
     "tsgb_bp_batch_workspace_bytes": (None, 2, 0),
+    "tsgb_fp_batch_workspace_bytes": (None, 2),
     "tsgb_projector_shapes": (None, None, None),
     "tsgb_projector_stats": (None, None, 8),
     "tsgb_projector_get_tuning": (None, None),

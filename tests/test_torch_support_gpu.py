@@ -214,3 +214,34 @@ def test_batched_backprojection_in_groups_equals_per_item(dev):
     for i in range(n):
         B.T(yy[i], out=ref_add[i])
     assert torch.equal(acc, ref_add)
+
+
+def test_batched_forward_projection_in_groups_equals_per_item(dev):
+    """A batched forward projection runs on multi-job launches (one ray launch
+    over up to 48 items, each with its own volume copies) when given the batch
+    workspace: 50 items equal projecting each on its own, bit for bit, setting
+    and adding, for both copy layouts."""
+    from tomosipo_gb300 import _native
+
+    vg = ts.volume(shape=(16, 18, 20), size=1)
+    pg = ts.cone(angles=9, shape=(16, 24), size=(1.2, 1.5), cone_angle=0.4)
+    A = ts.operator(vg, pg)
+    lib = _native.load()
+    h = A.projector.handle(dev.index)
+    assert lib.tsgb_fp_batch_workspace_bytes(h, 50) > lib.tsgb_fp_workspace_bytes(h)
+    n = 50
+    x = torch.rand(n, *A.domain_shape, device=dev)
+    B = ts.operator(vg, pg, additive=True)
+    for layout in (0, 1):
+        for op in (A, B):
+            op.projector.set_tuning(dev.index, fp_pair_layout=layout)
+        out = torch.full((n, *A.range_shape), 3.0, device=dev)
+        A._apply_batch(x, out)
+        ref = torch.stack([A(x[i]) for i in range(n)])
+        assert torch.equal(out, ref), layout
+        acc = ref.clone()
+        B._apply_batch(x, acc)
+        ref_add = ref.clone()
+        for i in range(n):
+            B(x[i], out=ref_add[i])
+        assert torch.equal(acc, ref_add), layout

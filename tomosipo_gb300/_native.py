@@ -74,6 +74,7 @@ SIGNATURES = {
     "tsgb_bp_workspace_bytes": (ctypes.c_int64, [ctypes.c_void_p, ctypes.c_int32]),
     "tsgb_bp_batch_workspace_bytes": (ctypes.c_int64, [ctypes.c_void_p, ctypes.c_int64,
                                                        ctypes.c_int32]),
+    "tsgb_fp_batch_workspace_bytes": (ctypes.c_int64, [ctypes.c_void_p, ctypes.c_int64]),
     "tsgb_direct_fp": (
         ctypes.c_int,
         [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int32, ctypes.c_void_p,

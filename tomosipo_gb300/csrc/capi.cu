@@ -251,6 +251,12 @@ int tsgb_direct_bp(tsgb_projector* p, float* vol, const float* sino, int32_t add
   return TSGB_OK;
 }
 
+int64_t tsgb_fp_batch_workspace_bytes(const tsgb_projector* p, int64_t n) {
+  const int64_t one = tsgb_fp_workspace_bytes(p);
+  if (one <= 0 || n <= 1 || p->fine || !tsgb::fp_multi_eligible(p)) return one;
+  return std::min<int64_t>(n, tsgb::kMaxMultiJobs) * one;
+}
+
 int tsgb_direct_fp_batch(tsgb_projector* p, const float* vol, float* sino, int64_t n,
                          int32_t additive, void* workspace, int64_t workspace_bytes,
                          void* stream) {
@@ -258,6 +264,18 @@ int tsgb_direct_fp_batch(tsgb_projector* p, const float* vol, float* sino, int64
   if (!p || !vol || !sino || n < 0) return fail(TSGB_ERR_INVALID, "NULL projector or data pointer");
   const size_t vol_elems = size_t(p->g.nz) * p->g.ny * p->g.nx;
   const size_t sino_elems = size_t(p->g.rows) * p->g.nangles * p->g.cols;
+  // multi-job launches when the workspace holds the volume copies of every
+  // item of a group (tsgb_fp_batch_workspace_bytes); else one after another
+  const int64_t one = tsgb_fp_workspace_bytes(p);
+  if (n > 1 && one > 0 && !p->fine && tsgb::fp_multi_eligible(p) && workspace &&
+      workspace_bytes >= tsgb_fp_batch_workspace_bytes(p, n)) {
+    int rc = check_device(p);
+    if (rc != TSGB_OK) return rc;
+    cudaError_t e = cudaError_t(tsgb::launch_fp_batch(p, vol, sino, n, additive != 0,
+                                                      static_cast<char*>(workspace), one, stream));
+    if (e != cudaSuccess) return cuda_fail(e, "batched forward projection launch");
+    return TSGB_OK;
+  }
   // one workspace serves every item: the projections run one after another on
   // the stream
   for (int64_t i = 0; i < n; ++i) {

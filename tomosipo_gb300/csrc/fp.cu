@@ -403,14 +403,14 @@ __global__ void __launch_bounds__(kFpRows* kFpCols, 4)
 
 // SIRT forward projections of many jobs in one launch: block b runs tile
 // b - start[j] of job j, exactly as fp_ray_kernel would for that job alone.
-template <typename E>
+template <bool kSirt, typename E>
 __global__ void __launch_bounds__(kFpRows* kFpCols, 4)
     fp_ray_multi_kernel(const __grid_constant__ FpMulti m) {
   __shared__ volatile long long out_slot[kFpRows * kFpCols];
   const int j = multi_job_of(m.start, m.n, blockIdx.x);
   const FpMultiJob& J = m.job[j];
-  fp_ray_tile<true, E>(J.params, J.columns, static_cast<const E*>(J.ws), nullptr, J.g, J.sched, 0,
-                       J.g.nangles, 0, J.sirt, blockIdx.x - m.start[j], out_slot);
+  fp_ray_tile<kSirt, E>(J.params, J.columns, static_cast<const E*>(J.ws), J.sino, J.g, J.sched,
+                        0, J.g.nangles, J.additive, J.sirt, blockIdx.x - m.start[j], out_slot);
 }
 
 }  // namespace
@@ -482,14 +482,49 @@ bool fp_multi_eligible(const tsgb_projector* p) {
          per_pair * ((p->g.nangles + 1) / 2) < (1LL << 31) / kMaxMultiJobs;
 }
 
-int launch_fp_multi(const FpMulti& m, bool pair_layout, void* stream_) {
+int launch_fp_multi(const FpMulti& m, bool pair_layout, void* stream_, bool sirt) {
   cudaStream_t stream = static_cast<cudaStream_t>(stream_);
   const long long blocks = m.start[m.n];
   if (blocks <= 0) return int(cudaGetLastError());
-  if (pair_layout)
-    fp_ray_multi_kernel<float2><<<unsigned(blocks), dim3(kFpRows, kFpCols), 0, stream>>>(m);
+  const dim3 block(kFpRows, kFpCols);
+  if (sirt && pair_layout)
+    fp_ray_multi_kernel<true, float2><<<unsigned(blocks), block, 0, stream>>>(m);
+  else if (sirt)
+    fp_ray_multi_kernel<true, float><<<unsigned(blocks), block, 0, stream>>>(m);
+  else if (pair_layout)
+    fp_ray_multi_kernel<false, float2><<<unsigned(blocks), block, 0, stream>>>(m);
   else
-    fp_ray_multi_kernel<float><<<unsigned(blocks), dim3(kFpRows, kFpCols), 0, stream>>>(m);
+    fp_ray_multi_kernel<false, float><<<unsigned(blocks), block, 0, stream>>>(m);
+  return int(cudaGetLastError());
+}
+
+int launch_fp_batch(const tsgb_projector* p, const float* vol, float* sino, int64_t n,
+                    bool additive, char* workspace, int64_t item_bytes, void* stream) {
+  const DeviceGeometry& g = p->g;
+  const size_t vol_elems = size_t(g.nz) * g.ny * g.nx;
+  const size_t sino_elems = size_t(g.rows) * g.nangles * g.cols;
+  for (int64_t i0 = 0; i0 < n; i0 += kMaxMultiJobs) {
+    const int m = int(std::min<int64_t>(kMaxMultiJobs, n - i0));
+    FpMulti fm{};
+    for (int k = 0; k < m; ++k) {
+      float* ws = reinterpret_cast<float*>(workspace + k * item_bytes);
+      const int rc = launch_fp_copies(p, vol + (i0 + k) * vol_elems, ws, stream);
+      if (rc != 0) return rc;
+      FpMultiJob& J = fm.job[k];
+      J.params = p->d_params;
+      J.columns = p->d_columns;
+      J.ws = ws;
+      J.g = g;
+      J.sched = fp_schedule(p, (g.nangles + 1) / 2);
+      J.sirt = FpSirt{};
+      J.sino = sino + (i0 + k) * sino_elems;
+      J.additive = additive ? 1 : 0;
+      fm.start[k + 1] = fm.start[k] + fp_blocks(p);
+    }
+    fm.n = m;
+    const int rc = launch_fp_multi(fm, p->tuning.fp_pair_layout != 0, stream, false);
+    if (rc != 0) return rc;
+  }
   return int(cudaGetLastError());
 }
 

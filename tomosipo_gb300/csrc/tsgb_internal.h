@@ -209,7 +209,9 @@ struct FpMultiJob {
   const void* ws;  // the job's padded volume copies
   DeviceGeometry g;
   FpSchedule sched;
-  FpSirt sirt;
+  FpSirt sirt;     // SIRT launches: where the residual goes
+  float* sino;     // plain launches: the job's sinogram (= or += when additive)
+  int additive;
 };
 struct FpMulti {
   int n;
@@ -243,7 +245,13 @@ int launch_fp_copies(const tsgb_projector* p, const float* vol, float* workspace
 // chunk), its block count, and the multi-job launch itself (fp.cu).
 bool fp_multi_eligible(const tsgb_projector* p);
 long long fp_blocks(const tsgb_projector* p);
-int launch_fp_multi(const FpMulti& m, bool pair_layout, void* stream);
+// sirt: each job writes its SIRT residual; else its sinogram.
+int launch_fp_multi(const FpMulti& m, bool pair_layout, void* stream, bool sirt = true);
+// Forward projection of n stacked volumes of one projector on multi-job
+// launches (fp_multi_eligible, no supersampling): item k's volume copies at
+// workspace + (k % kMaxMultiJobs) * item_bytes, groups of kMaxMultiJobs (fp.cu).
+int launch_fp_batch(const tsgb_projector* p, const float* vol, float* sino, int64_t n,
+                    bool additive, char* workspace, int64_t item_bytes, void* stream);
 // Blocks of one voxel-pair backprojection pass of a job (gx, gy set), and
 // the multi-job launch of that pass over several jobs (bp.cu).
 long long bp_sep_blocks(const tsgb_projector* p, bool a_is_x, int* gx, int* gy);

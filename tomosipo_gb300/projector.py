@@ -437,12 +437,13 @@ def direct_project_batch(projector, vol, sino, forward, additive=False, bp_kind=
     with torch.cuda.device(device):
         h = projector.handle(device.index)
         stream = torch.cuda.current_stream(device).cuda_stream
+        # per-item volume copies / weighted sinograms let the items share launches
         if forward:
-            nbytes = projector.workspace_bytes(device.index, forward, bp_kind)
-        else:  # a weighted sinogram per item lets the items share launches
+            nbytes = int(lib.tsgb_fp_batch_workspace_bytes(h, n))
+        else:
             nbytes = int(lib.tsgb_bp_batch_workspace_bytes(h, n, BP_KINDS[bp_kind]))
-            if nbytes < 0:
-                _native.check(int(nbytes), "tsgb_bp_batch_workspace_bytes")
+        if nbytes < 0:
+            _native.check(nbytes, "batch workspace query")
         ws = torch.empty(max(nbytes, 1), dtype=torch.uint8, device=device)
         if forward:
             rc = lib.tsgb_direct_fp_batch(h, vol.data_ptr(), sino.data_ptr(), n, int(bool(additive)),
