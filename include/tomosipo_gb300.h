@@ -100,8 +100,10 @@ int tsgb_direct_bp(tsgb_projector* p, float* vol, const float* sino,
  * as tsgb_direct_fp (equal results), in one call. Replaces the per-slice loop
  * over batch and channel dimensions of tomosipo's to_autograd
  * (tomosipo/torch_support.py:49-53). With a workspace of
- * tsgb_fp_batch_workspace_bytes(p, n) bytes (volume copies per item), the
- * items run on multi-job launches (one ray launch over up to 48 items); with
+ * tsgb_fp_batch_workspace_bytes(p, n) bytes, the items run on multi-job
+ * launches: one ray launch over as many items as the workspace holds volume
+ * copies for (up to 48; the query keeps that within 2 GiB, so projectors
+ * whose copies are larger run one item after another); with
  * tsgb_fp_workspace_bytes, one after another on ``stream``. */
 int64_t tsgb_fp_batch_workspace_bytes(const tsgb_projector* p, int64_t n);
 int tsgb_direct_fp_batch(tsgb_projector* p, const float* vol, float* sino, int64_t n,
@@ -114,8 +116,10 @@ int tsgb_direct_fp_batch(tsgb_projector* p, const float* vol, float* sino, int64
  * (tomosipo/torch_support.py:70-74). With a workspace of
  * tsgb_bp_batch_workspace_bytes(p, n, bp_kind) bytes, matched
  * backprojections of the voxel-pair kernel run on multi-job launches (one
- * launch per pass over up to 48 items, which fill the GPU where one small
- * volume does not); with tsgb_bp_workspace_bytes, one item after another. */
+ * launch per pass over as many items as the workspace holds weighted
+ * sinograms for, up to 48; they fill the GPU where one small volume does not;
+ * the query keeps the workspace within 2 GiB); otherwise one item after
+ * another. */
 int64_t tsgb_bp_batch_workspace_bytes(const tsgb_projector* p, int64_t n, int32_t bp_kind);
 int tsgb_direct_bp_batch(tsgb_projector* p, float* vol, const float* sino, int64_t n,
                          int32_t additive, int32_t bp_kind, void* workspace,

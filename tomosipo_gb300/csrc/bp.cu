@@ -1314,14 +1314,15 @@ bool bp_batch_multi_eligible(const tsgb_projector* p) {
 }
 
 int launch_bp_matched_batch(const tsgb_projector* p, float* vol, const float* sino, int64_t n,
-                            bool additive, char* workspace, int64_t item_bytes, void* stream_) {
+                            bool additive, char* workspace, int64_t item_bytes, int group,
+                            void* stream_) {
   cudaStream_t stream = static_cast<cudaStream_t>(stream_);
   const DeviceGeometry& g = p->g;
   const size_t vol_elems = size_t(g.nz) * g.ny * g.nx;
   const size_t sino_elems = size_t(g.rows) * g.nangles * g.cols;
   const int n_ax = p->n_sep_ax, n_ay = p->n_separable_bp - p->n_sep_ax;
-  for (int64_t i0 = 0; i0 < n; i0 += kMaxMultiJobs) {
-    const int m = int(std::min<int64_t>(kMaxMultiJobs, n - i0));
+  for (int64_t i0 = 0; i0 < n; i0 += group) {
+    const int m = int(std::min<int64_t>(group, n - i0));
     for (int k = 0; k < m; ++k)
       launch_bp_weight_rows(p, sino + (i0 + k) * sino_elems,
                             reinterpret_cast<float2*>(workspace + k * item_bytes), 0, g.nangles,

@@ -254,7 +254,8 @@ int tsgb_direct_bp(tsgb_projector* p, float* vol, const float* sino, int32_t add
 int64_t tsgb_fp_batch_workspace_bytes(const tsgb_projector* p, int64_t n) {
   const int64_t one = tsgb_fp_workspace_bytes(p);
   if (one <= 0 || n <= 1 || p->fine || !tsgb::fp_multi_eligible(p)) return one;
-  return std::min<int64_t>(n, tsgb::kMaxMultiJobs) * one;
+  const int64_t group = tsgb::batch_group(n, one);
+  return group > 1 ? group * one : one;
 }
 
 int tsgb_direct_fp_batch(tsgb_projector* p, const float* vol, float* sino, int64_t n,
@@ -267,12 +268,15 @@ int tsgb_direct_fp_batch(tsgb_projector* p, const float* vol, float* sino, int64
   // multi-job launches when the workspace holds the volume copies of every
   // item of a group (tsgb_fp_batch_workspace_bytes); else one after another
   const int64_t one = tsgb_fp_workspace_bytes(p);
-  if (n > 1 && one > 0 && !p->fine && tsgb::fp_multi_eligible(p) && workspace &&
-      workspace_bytes >= tsgb_fp_batch_workspace_bytes(p, n)) {
+  const int64_t group = one > 0 && workspace ? std::min<int64_t>({n, int64_t(tsgb::kMaxMultiJobs),
+                                                                 workspace_bytes / one})
+                                             : 0;
+  if (group > 1 && !p->fine && tsgb::fp_multi_eligible(p)) {
     int rc = check_device(p);
     if (rc != TSGB_OK) return rc;
     cudaError_t e = cudaError_t(tsgb::launch_fp_batch(p, vol, sino, n, additive != 0,
-                                                      static_cast<char*>(workspace), one, stream));
+                                                      static_cast<char*>(workspace), one,
+                                                      int(group), stream));
     if (e != cudaSuccess) return cuda_fail(e, "batched forward projection launch");
     return TSGB_OK;
   }
@@ -290,8 +294,8 @@ int64_t tsgb_bp_batch_workspace_bytes(const tsgb_projector* p, int64_t n, int32_
   const int64_t one = tsgb_bp_workspace_bytes(p, bp_kind);
   if (one < 0 || n <= 1 || bp_kind != TSGB_BP_MATCHED || !tsgb::bp_batch_multi_eligible(p))
     return one;
-  return std::max<int64_t>(one, std::min<int64_t>(n, tsgb::kMaxMultiJobs) *
-                                    tsgb::bp_pairs_bytes(p->g));
+  const int64_t item = tsgb::bp_pairs_bytes(p->g), group = tsgb::batch_group(n, item);
+  return group > 1 ? std::max<int64_t>(one, group * item) : one;
 }
 
 int tsgb_direct_bp_batch(tsgb_projector* p, float* vol, const float* sino, int64_t n,
@@ -303,13 +307,15 @@ int tsgb_direct_bp_batch(tsgb_projector* p, float* vol, const float* sino, int64
   const size_t sino_elems = size_t(p->g.rows) * p->g.nangles * p->g.cols;
   // multi-job launches when the workspace holds a weighted sinogram per item
   // of a group (tsgb_bp_batch_workspace_bytes); else one item after another
-  if (n > 1 && bp_kind == TSGB_BP_MATCHED && tsgb::bp_batch_multi_eligible(p) && workspace &&
-      workspace_bytes >= tsgb_bp_batch_workspace_bytes(p, n, bp_kind)) {
+  const int64_t item = tsgb::bp_pairs_bytes(p->g);
+  const int64_t group = workspace ? std::min<int64_t>({n, int64_t(tsgb::kMaxMultiJobs),
+                                                       workspace_bytes / item})
+                                  : 0;
+  if (group > 1 && bp_kind == TSGB_BP_MATCHED && tsgb::bp_batch_multi_eligible(p)) {
     int rc = check_device(p);
     if (rc != TSGB_OK) return rc;
     cudaError_t e = cudaError_t(tsgb::launch_bp_matched_batch(
-        p, vol, sino, n, additive != 0, static_cast<char*>(workspace), tsgb::bp_pairs_bytes(p->g),
-        stream));
+        p, vol, sino, n, additive != 0, static_cast<char*>(workspace), item, int(group), stream));
     if (e != cudaSuccess) return cuda_fail(e, "batched backprojection launch");
     return TSGB_OK;
   }

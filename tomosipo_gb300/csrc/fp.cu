@@ -499,12 +499,12 @@ int launch_fp_multi(const FpMulti& m, bool pair_layout, void* stream_, bool sirt
 }
 
 int launch_fp_batch(const tsgb_projector* p, const float* vol, float* sino, int64_t n,
-                    bool additive, char* workspace, int64_t item_bytes, void* stream) {
+                    bool additive, char* workspace, int64_t item_bytes, int group, void* stream) {
   const DeviceGeometry& g = p->g;
   const size_t vol_elems = size_t(g.nz) * g.ny * g.nx;
   const size_t sino_elems = size_t(g.rows) * g.nangles * g.cols;
-  for (int64_t i0 = 0; i0 < n; i0 += kMaxMultiJobs) {
-    const int m = int(std::min<int64_t>(kMaxMultiJobs, n - i0));
+  for (int64_t i0 = 0; i0 < n; i0 += group) {
+    const int m = int(std::min<int64_t>(group, n - i0));
     FpMulti fm{};
     for (int k = 0; k < m; ++k) {
       float* ws = reinterpret_cast<float*>(workspace + k * item_bytes);

@@ -335,9 +335,10 @@ std::string build_plan(const tsgb_volume_desc* vol, const tsgb_projection_desc* 
     ap.vs_b = float(vs[L.b]);
   }
   p->fp_workspace_elems = off;
-  // Most of the separable work on rows finer than the voxels (a supersampled
-  // or fine detector; about 0.6 % of it for the cone scans of the benchmark):
-  // the matched backprojection takes the voxel-pair kernel's fine-row variant.
+  // At least a quarter of the separable work on rows finer than the voxels (a
+  // supersampled or fine detector; about 0.6 % of it for the cone scans of the
+  // benchmark): the matched backprojection takes the voxel-pair kernel's
+  // fine-row variant.
   p->fine_rows = all_planes > 0.0 && fine_planes >= 0.25 * all_planes;
   p->n_general_bp = int(gen_angles->size());
   // Separable angles grouped by their in-plane axis a (x first, then y): the

@@ -19,6 +19,7 @@
 // The matched backprojection is the exact transpose of this.
 #pragma once
 
+#include <algorithm>
 #include <cstdint>
 #include <string>
 #include <vector>
@@ -202,6 +203,15 @@ struct FpSirt {
 // b running block b - start[j] of job j (start[j] <= b < start[j + 1]). The job
 // descriptors travel as __grid_constant__ kernel arguments.
 constexpr int kMaxMultiJobs = 48;
+// Batched projections share multi-job launches in groups of items whose
+// per-item workspaces (volume copies, weighted sinograms) fit this budget: the
+// launches pay off for items too small to fill the GPU alone.
+constexpr int64_t kBatchWorkspaceBudget = int64_t(2) << 30;
+inline int64_t batch_group(int64_t n, int64_t item_bytes) {
+  if (item_bytes <= 0) return 1;
+  const int64_t fit = kBatchWorkspaceBudget / item_bytes;
+  return std::max<int64_t>(1, std::min<int64_t>({n, int64_t(kMaxMultiJobs), fit}));
+}
 
 struct FpMultiJob {
   const AngleParams* params;
@@ -248,10 +258,11 @@ long long fp_blocks(const tsgb_projector* p);
 // sirt: each job writes its SIRT residual; else its sinogram.
 int launch_fp_multi(const FpMulti& m, bool pair_layout, void* stream, bool sirt = true);
 // Forward projection of n stacked volumes of one projector on multi-job
-// launches (fp_multi_eligible, no supersampling): item k's volume copies at
-// workspace + (k % kMaxMultiJobs) * item_bytes, groups of kMaxMultiJobs (fp.cu).
+// launches (fp_multi_eligible, no supersampling), `group` items per launch
+// (<= kMaxMultiJobs): item k's volume copies at workspace + (k % group) *
+// item_bytes (fp.cu).
 int launch_fp_batch(const tsgb_projector* p, const float* vol, float* sino, int64_t n,
-                    bool additive, char* workspace, int64_t item_bytes, void* stream);
+                    bool additive, char* workspace, int64_t item_bytes, int group, void* stream);
 // Blocks of one voxel-pair backprojection pass of a job (gx, gy set), and
 // the multi-job launch of that pass over several jobs (bp.cu).
 long long bp_sep_blocks(const tsgb_projector* p, bool a_is_x, int* gx, int* gy);
@@ -259,11 +270,12 @@ int launch_bp_sep_multi(const BpMulti& m, bool a_is_x, void* stream);
 // Whether a projector's batched matched backprojection can run on multi-job
 // launches (voxel-pair kernel, separable angles only, 32-bit offsets, no
 // supersampling or fine-row variant), and that batched backprojection:
-// n items, item k's weighted sinogram at workspace + (k % kMaxMultiJobs) *
-// item_bytes (item_bytes >= bp_pairs_bytes), in groups of kMaxMultiJobs (bp.cu).
+// `group` items per launch (<= kMaxMultiJobs), item k's weighted sinogram at
+// workspace + (k % group) * item_bytes (item_bytes >= bp_pairs_bytes) (bp.cu).
 bool bp_batch_multi_eligible(const tsgb_projector* p);
 int launch_bp_matched_batch(const tsgb_projector* p, float* vol, const float* sino, int64_t n,
-                            bool additive, char* workspace, int64_t item_bytes, void* stream);
+                            bool additive, char* workspace, int64_t item_bytes, int group,
+                            void* stream);
 
 // The matched backprojector of det_v-along-z angles is the z-lane kernel
 // (bp_zlane.cu, column-major weighted sinogram) unless the tuning picks the
