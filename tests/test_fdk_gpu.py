@@ -28,6 +28,12 @@ def dev(native_lib):
 
 CASES = {
     "cone": (ts.volume(shape=24, size=1), ts.cone(angles=40, shape=(24, 36), size=np.sqrt(2), cone_angle=0.5)),
+    # the benchmark's cone family (unit cube, sqrt(2) detector, cone angle 0.5)
+    # at 64^3, 64 angles, 64 x 96
+    "cone_64_benchmark_family": (
+        ts.volume(shape=64, size=1),
+        ts.cone(angles=64, shape=(64, 96), size=np.sqrt(2), cone_angle=0.5),
+    ),
     "cone_aniso_offset": (
         ts.volume(shape=(20, 24, 28), size=(0.8, 1.0, 1.1), pos=(0.02, -0.05, 0.04)),
         ts.cone(angles=30, shape=(22, 40), size=(1.2, 2.0), src_orig_dist=3.0, src_det_dist=4.5),

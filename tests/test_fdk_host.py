@@ -114,3 +114,16 @@ def test_fft_length_avoids_wrap_around_with_fast_radices(cols):
 def test_fdk_rejects_parallel_beams():
     with pytest.raises(ValueError):
         fdk.fdk_constants(ts.volume(shape=4), ts.parallel(angles=3, shape=4))
+
+
+@pytest.mark.parametrize("scan", ["circular", "jittered"])
+def test_filter_does_not_depend_on_the_angle_chunk(scan):
+    """The filter runs its angles in chunks (as many as fit its buffer budget);
+    every angle's arithmetic is the same whatever the chunk, so chunks of 1, 5
+    and all 17 angles give equal results."""
+    pg = _scans()[scan]
+    vg = ts.volume(shape=(10, 12, 14), size=(0.8, 1, 1.1), pos=(0.05, -0.1, 0.02))
+    y = torch.from_numpy(np.random.default_rng(2).random((9, 17, 13)).astype(np.float32))
+    ref = fdk.fdk_filter(vg, pg, y, angle_chunk=17)
+    for chunk in (1, 5, None):
+        assert torch.equal(fdk.fdk_filter(vg, pg, y, angle_chunk=chunk), ref), chunk
