@@ -479,11 +479,14 @@ __global__ void __launch_bounds__(128)
 // nothing), so both give the same result. Where a region would not fit (a
 // detector much finer than the voxels, or a source inside the box's reach), the
 // box falls back to general_voxel_terms for that angle.
-constexpr int kGenBoxZ = 16, kGenBoxY = 8, kGenBoxX = 16;  // voxels per block
-// voxels along x per thread: 8 measured 41.4 ms at 256^3 / 360 tilted angles,
-// 4 (boxes of 16 x 8 x 8) 47.0 ms, 16 (80 registers, 3 blocks per SM) 44.2 ms
-constexpr int kGenRunX = 8;
-constexpr int kGenThreads = kGenBoxZ * kGenBoxY * kGenBoxX / kGenRunX;  // 256
+// Boxes of 16 (z) x 8 (y) x 2 kRunX (x) voxels, kRunX voxels along x per
+// thread (the kernel's template argument). kRunX = 8 measured 41.4 ms at
+// 256^3 / 360 tilted angles, 4 (boxes of 16 x 8 x 8) 47.0 ms, 16 (80
+// registers, 3 blocks per SM) 44.2 ms; the launcher takes 4 where a 16-wide
+// box's detector region would not fit the stage (detectors finer than the
+// voxels), since those angles would fall back to the per-voxel sums.
+constexpr int kGenBoxZ = 16, kGenBoxY = 8;
+constexpr int kGenThreads = 256;
 constexpr int kGenStage = 2048;                           // staged pixels per angle
 constexpr int kGenWindow = 9;  // largest box-wide window (pixels) summed by every voxel
 
@@ -564,7 +567,7 @@ __device__ __forceinline__ void gen_region(const AngleParams& ap, const DeviceGe
     r.nv = v1 - v0 + 1;
     // staged in the sinogram's own order, so the staging reads are coalesced,
     // with an odd stride between columns (rows) so that the two half-warps,
-    // eight voxels apart along x, read different banks
+    // kGenRunX voxels apart along x, read different banks
     const int inner = zlayout ? r.nv : r.nu, outer = zlayout ? r.nu : r.nv;
     const int stride = inner | 1;
     if (r.nu <= 0 || r.nv <= 0)
@@ -596,6 +599,7 @@ __device__ __forceinline__ void gen_region(const AngleParams& ap, const DeviceGe
   *out = r;
 }
 
+template <int kGenRunX>
 __global__ void __launch_bounds__(kGenThreads, 4)
     bp_general_box_kernel(const AngleParams* __restrict__ params,
                           const ColumnEntry* __restrict__ columns,
@@ -606,6 +610,8 @@ __global__ void __launch_bounds__(kGenThreads, 4)
   __shared__ float s_val[kGenStage];   // W y
   __shared__ GenRegion s_reg[2];       // regions of angles n and n + 1
   const int tid = threadIdx.x, warp = tid >> 5;
+  constexpr int kGenBoxX = 2 * kGenRunX;
+  static_assert(kGenBoxZ * kGenBoxY * kGenBoxX / kGenRunX == kGenThreads, "one thread per x run");
   const int bz = blockIdx.z * kGenBoxZ, by = blockIdx.y * kGenBoxY, bx = blockIdx.x * kGenBoxX;
   // this thread's voxels: (z, y, x0 + m), m < kGenRunX
   const int z = bz + (tid & 15), y = by + (tid >> 5), x0 = bx + ((tid >> 4) & 1) * kGenRunX;
@@ -791,11 +797,15 @@ void launch_bp_general(const tsgb_projector* p, const int* angles, int n, const 
                                                         zlayout ? 1 : 0);
     return;
   }
-  const dim3 grid((g.nx + kGenBoxX - 1) / kGenBoxX, (g.ny + kGenBoxY - 1) / kGenBoxY,
+  const int run = p->gen_box_wide ? 8 : 4, box_x = 2 * run;
+  const dim3 grid((g.nx + box_x - 1) / box_x, (g.ny + kGenBoxY - 1) / kGenBoxY,
                   (g.nz + kGenBoxZ - 1) / kGenBoxZ);
-  bp_general_box_kernel<<<grid, kGenThreads, 0, stream>>>(p->d_params, p->d_columns, angles, n,
-                                                          pairs, vol, g, additive ? 1 : 0,
-                                                          zlayout ? 1 : 0);
+  if (run == 8)
+    bp_general_box_kernel<8><<<grid, kGenThreads, 0, stream>>>(
+        p->d_params, p->d_columns, angles, n, pairs, vol, g, additive ? 1 : 0, zlayout ? 1 : 0);
+  else
+    bp_general_box_kernel<4><<<grid, kGenThreads, 0, stream>>>(
+        p->d_params, p->d_columns, angles, n, pairs, vol, g, additive ? 1 : 0, zlayout ? 1 : 0);
 }
 
 // Bilinear detector value at anchored (ut, vt), zero outside the detector.

@@ -340,6 +340,41 @@ std::string build_plan(const tsgb_volume_desc* vol, const tsgb_projection_desc* 
   // benchmark): the matched backprojection takes the voxel-pair kernel's
   // fine-row variant.
   p->fine_rows = all_planes > 0.0 && fine_planes >= 0.25 * all_planes;
+  // Detector region of a 16 x 8 x 16 voxel box at the anchor for each general
+  // angle (its corners widened by one voxel along a and b, as the kernel
+  // does; pixels from floor(min) to ceil(max) of their projections, an odd
+  // stride): boxes nearer a cone's source project larger, hence the margin.
+  p->gen_box_wide = true;
+  for (int t : *gen_angles) {
+    const AngleParams& ap = p->host_params[t];
+    const double lo[3] = {-8.0, -4.0, -8.0}, hi[3] = {7.0, 3.0, 7.0};
+    double umin = 1e300, umax = -1e300, vmin = 1e300, vmax = -1e300;
+    bool ok = true;
+    for (int c = 0; c < 8; ++c) {
+      double P[3];
+      for (int ax = 0; ax < 3; ++ax) {
+        const double e = ax == ap.d ? 0.0 : 1.0;
+        P[ax] = ((c >> ax) & 1) ? hi[ax] + e : lo[ax] - e;
+      }
+      const double nu = ap.pu[0] * P[0] + ap.pu[1] * P[1] + ap.pu[2] * P[2] + ap.pu[3];
+      const double nv = ap.pv[0] * P[0] + ap.pv[1] * P[1] + ap.pv[2] * P[2] + ap.pv[3];
+      const double nw = ap.pw[0] * P[0] + ap.pw[1] * P[1] + ap.pw[2] * P[2] + ap.pw[3];
+      if (!(nw > 0.0)) {
+        ok = false;
+        break;
+      }
+      umin = std::min(umin, nu / nw);
+      umax = std::max(umax, nu / nw);
+      vmin = std::min(vmin, nv / nw);
+      vmax = std::max(vmax, nv / nw);
+    }
+    const double nu = std::ceil(umax) - std::floor(umin) + 1.0;
+    const double nv = std::ceil(vmax) - std::floor(vmin) + 1.0;
+    if (!ok || 1.5 * (nu + 1.0) * (nv + 1.0) > 2048.0) {
+      p->gen_box_wide = false;
+      break;
+    }
+  }
   p->n_general_bp = int(gen_angles->size());
   // Separable angles grouped by their in-plane axis a (x first, then y): the
   // backprojector runs one pass per group, each with voxel runs along a.

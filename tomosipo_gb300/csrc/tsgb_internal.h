@@ -125,6 +125,11 @@ struct tsgb_projector {
   // the matched backprojection then runs the voxel-pair kernel's fine-row
   // variant.
   bool fine_rows = false;
+  // The general backprojector's voxel boxes may be 16 wide along x: the
+  // detector region a 16 x 8 x 16 box at the volume's centre projects to, for
+  // every general angle, stays within two thirds of the kernel's stage (else
+  // boxes 8 wide, whose regions are about half as large).
+  bool gen_box_wide = true;
   int n_bil_fast = 0;           // bilinear BP: angles for the z-flat kernel
   int n_bil_slow = 0;           // bilinear BP: angles for the general kernel
   tsgb::AngleParams* d_params = nullptr;
