@@ -10,7 +10,9 @@ Cases cover both weighted-sinogram layouts (bp_kernel 0: row-major pairs,
 1: column-major), the additive form, volumes that are not whole boxes, a scan
 that mixes separable and tilted angles (the general kernel adds onto the
 separable passes), and the box kernel's three ways of summing: a box-wide
-window of candidate pixels (pixels about as large as voxels), a bound per
+window of candidate pixels (pixels about as large as voxels; unrolled sums for
+windows of 3 x 2, 2 x 2, 3 x 3 and 2 x 3 pixels, loops for other shapes such
+as 4 x 1 or 1 x 6, which the cases with oblong pixels reach), a bound per
 voxel (footprints wider than that window), and, for a detector fine enough
 that the staged region does not fit, the per-voxel sums.
 """
@@ -54,6 +56,22 @@ def _cases():
         "finer_detector_bounds": (
             ts.volume(shape=24, size=1),
             R * ts.cone(angles=5, shape=(60, 75), size=1.6, src_orig_dist=2.5,
+                        src_det_dist=3.5).to_vec(),
+        ),
+        # pixels four times taller than wide (0.16 x 0.04 of a 24-voxel unit
+        # volume): box-wide windows of 4 x 1, 4 x 2 and 3 x 1 pixels, which
+        # take the window loops sized at run time
+        "tall_pixel_windows": (
+            ts.volume(shape=24, size=1),
+            R * ts.cone(angles=5, shape=(10, 40), size=1.6, src_orig_dist=2.5,
+                        src_det_dist=3.5).to_vec(),
+        ),
+        # pixels about four times wider than tall: windows of 1 x 5 and 1 x 6
+        # pixels (wu * 4 + wv of a 1 x 6 window equals that of 2 x 2, so a
+        # shape key of that form would sum the wrong window here)
+        "wide_pixel_windows": (
+            ts.volume(shape=24, size=1),
+            R * ts.cone(angles=5, shape=(60, 14), size=1.6, src_orig_dist=2.5,
                         src_det_dist=3.5).to_vec(),
         ),
         # pixels ~4x finer than voxels: a box's region exceeds the stage
