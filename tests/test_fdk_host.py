@@ -127,3 +127,6 @@ def test_filter_does_not_depend_on_the_angle_chunk(scan):
     ref = fdk.fdk_filter(vg, pg, y, angle_chunk=17)
     for chunk in (1, 5, None):
         assert torch.equal(fdk.fdk_filter(vg, pg, y, angle_chunk=chunk), ref), chunk
+    for bad in (0, -3):
+        with pytest.raises(ValueError, match="angle_chunk"):
+            fdk.fdk_filter(vg, pg, y, angle_chunk=bad)

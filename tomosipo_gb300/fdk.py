@@ -184,6 +184,9 @@ def fdk_filter(vg, pg, y, angle_chunk=None, short_scan=False):
     dev = y.device
     if angle_chunk is None:
         angle_chunk = max(1, (512 << 20) // (rows * fft_length(cols) * 4))
+    elif int(angle_chunk) < 1:
+        raise ValueError(f"angle_chunk must be a positive number of angles, got {angle_chunk}")
+    angle_chunk = int(angle_chunk)
     sdd, pitch, _ = fdk_constants(vg, pg)
     S, D, U, V = _vectors(pg)
     parker = (torch.from_numpy(short_scan_weights(vg, pg).astype(np.float32)).to(dev)
